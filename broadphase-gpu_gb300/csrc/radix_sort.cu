@@ -1,0 +1,256 @@
+// radix_sort.cu - stable LSD radix sort on the device.
+//
+// Replaces the comparison sort of the reference (thrust::sort_by_key with
+// sort_aabb_x, src/simulation.cu:645-649, 277-293). Keys are the order-
+// preserving uint32 images of the sweep-axis minima; values are box indices.
+// Each pass is reduce-then-scan, with no inter-block waiting:
+//   upsweep   per-tile digit histogram          (reads keys)
+//   scan      per-digit exclusive scan over tiles, then over digit totals
+//   downsweep stable in-tile ranking (warp match_any + per-warp counters),
+//             staging in shared memory by digit, coalesced scatter
+#include "stq_device.cuh"
+#include "stq_internal.h"
+
+namespace stq {
+
+namespace {
+
+constexpr int kSortBlock = 256;
+constexpr int kSortWarps = kSortBlock / 32;
+
+template <typename K> struct TileShape {
+  static constexpr int items = sizeof(K) == 4 ? 16 : 8;
+  static constexpr int tile = kSortBlock * items;
+};
+
+int64_t num_tiles(int64_t n, int tile) { return (n + tile - 1) / tile; }
+
+template <typename K, int BITS>
+__global__ void __launch_bounds__(kSortBlock)
+upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift,
+               uint32_t *__restrict__ hist, int64_t ntiles) {
+  constexpr int BINS = 1 << BITS;
+  constexpr int TILE = TileShape<K>::tile;
+  __shared__ uint32_t h[kSortWarps][BINS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < kSortWarps * BINS; i += kSortBlock) (&h[0][0])[i] = 0;
+  __syncthreads();
+  const int64_t base = int64_t(blockIdx.x) * TILE;
+  for (int i = 0; i < TILE / kSortBlock; ++i) {
+    const int64_t idx = base + int64_t(i) * kSortBlock + threadIdx.x;
+    const int d = idx < n ? int((keys[idx] >> shift) & (BINS - 1)) : BINS;
+    const unsigned peers = __match_any_sync(kFullMask, d);
+    if (d < BINS && lane == __ffs(peers) - 1) atomicAdd(&h[warp][d], __popc(peers));
+  }
+  __syncthreads();
+  for (int d = threadIdx.x; d < BINS; d += kSortBlock) {
+    uint32_t s = 0;
+    for (int w = 0; w < kSortWarps; ++w) s += h[w][d];
+    hist[int64_t(d) * ntiles + blockIdx.x] = s;
+  }
+}
+
+// Block-wide exclusive scan of one value per thread (kSortBlock threads).
+__device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total, uint32_t *scratch) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t y = __shfl_up_sync(kFullMask, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) scratch[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t w = lane < kSortWarps ? scratch[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(kFullMask, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kSortWarps) scratch[lane] = w;  // inclusive warp totals
+  }
+  __syncthreads();
+  const uint32_t warp_base = warp > 0 ? scratch[warp - 1] : 0;
+  *total = scratch[kSortWarps - 1];
+  __syncthreads();
+  return warp_base + x - v;
+}
+
+// One block per digit: exclusive scan of hist[d][0..ntiles) in place.
+__global__ void __launch_bounds__(kSortBlock)
+scan_rows_kernel(uint32_t *__restrict__ hist, int64_t ntiles,
+                 uint32_t *__restrict__ totals) {
+  __shared__ uint32_t scratch[32];
+  uint32_t *row = hist + int64_t(blockIdx.x) * ntiles;
+  uint32_t carry = 0;
+  for (int64_t b = 0; b < ntiles; b += kSortBlock) {
+    const int64_t i = b + threadIdx.x;
+    const uint32_t v = i < ntiles ? row[i] : 0;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, &tot, scratch);
+    if (i < ntiles) row[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+}
+
+template <int BINS>
+__global__ void __launch_bounds__(kSortBlock)
+scan_totals_kernel(uint32_t *__restrict__ totals) {
+  __shared__ uint32_t scratch[32];
+  const uint32_t v = threadIdx.x < BINS ? totals[threadIdx.x] : 0;
+  uint32_t tot;
+  const uint32_t ex = block_exclusive_scan(v, &tot, scratch);
+  if (threadIdx.x < BINS) totals[threadIdx.x] = ex;
+}
+
+template <typename K, int BITS, bool VALS>
+__global__ void __launch_bounds__(kSortBlock)
+downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
+                 const uint32_t *__restrict__ vin, uint32_t *__restrict__ vout,
+                 int64_t n, int shift, const uint32_t *__restrict__ tile_off,
+                 const uint32_t *__restrict__ digit_base, int64_t ntiles) {
+  constexpr int BINS = 1 << BITS;
+  constexpr int ITEMS = TileShape<K>::items;
+  constexpr int TILE = TileShape<K>::tile;
+  __shared__ uint32_t cnt[kSortWarps][BINS + 1];
+  __shared__ uint32_t tile_prefix[BINS];
+  __shared__ uint32_t gbase[BINS];
+  __shared__ uint32_t scratch[32];
+  __shared__ K stage[TILE];
+  __shared__ uint8_t stage_d[TILE];
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t tile_start = int64_t(blockIdx.x) * TILE;
+  const int64_t wstart = tile_start + int64_t(warp) * 32 * ITEMS;
+  for (int i = threadIdx.x; i < kSortWarps * (BINS + 1); i += kSortBlock) (&cnt[0][0])[i] = 0;
+  __syncthreads();
+
+  K key[ITEMS];
+  uint32_t val[ITEMS];
+  int dig[ITEMS];
+  uint32_t rank[ITEMS];
+#pragma unroll
+  for (int it = 0; it < ITEMS; ++it) {
+    const int64_t idx = wstart + it * 32 + lane;
+    if (idx < n) {
+      key[it] = kin[idx];
+      if (VALS) val[it] = vin[idx];
+      dig[it] = int((key[it] >> shift) & (BINS - 1));
+    } else {
+      dig[it] = BINS;  // dummy bin: counted, never written
+    }
+  }
+  // Stable in-warp ranking: items in input order, lanes in input order.
+#pragma unroll
+  for (int it = 0; it < ITEMS; ++it) {
+    const unsigned peers = __match_any_sync(kFullMask, dig[it]);
+    const uint32_t base = cnt[warp][dig[it]];
+    __syncwarp();
+    if (lane == __ffs(peers) - 1) cnt[warp][dig[it]] = base + __popc(peers);
+    __syncwarp();
+    rank[it] = base + __popc(peers & lanemask_lt());
+  }
+  __syncthreads();
+  // Per digit: exclusive prefix over warps and the digit's tile total.
+  uint32_t dtotal = 0;
+  if (threadIdx.x < BINS) {
+    uint32_t run = 0;
+    for (int w = 0; w < kSortWarps; ++w) {
+      const uint32_t c = cnt[w][threadIdx.x];
+      cnt[w][threadIdx.x] = run;
+      run += c;
+    }
+    dtotal = run;
+  }
+  __syncthreads();
+  uint32_t tot;
+  const uint32_t ex = block_exclusive_scan(dtotal, &tot, scratch);
+  if (threadIdx.x < BINS) {
+    tile_prefix[threadIdx.x] = ex;
+    gbase[threadIdx.x] =
+        digit_base[threadIdx.x] + tile_off[int64_t(threadIdx.x) * ntiles + blockIdx.x];
+  }
+  __syncthreads();
+  // Stage keys in tile-sorted order, then write them out digit run by run.
+  int pos[ITEMS];
+#pragma unroll
+  for (int it = 0; it < ITEMS; ++it) {
+    if (dig[it] < BINS) {
+      pos[it] = int(tile_prefix[dig[it]] + cnt[warp][dig[it]] + rank[it]);
+      stage[pos[it]] = key[it];
+      stage_d[pos[it]] = uint8_t(dig[it]);
+    }
+  }
+  __syncthreads();
+  const int count = int(n - tile_start < TILE ? n - tile_start : TILE);
+  for (int p = threadIdx.x; p < count; p += kSortBlock) {
+    const int d = stage_d[p];
+    kout[gbase[d] + (p - tile_prefix[d])] = stage[p];
+  }
+  if (VALS) {
+    __syncthreads();
+    uint32_t *vstage = reinterpret_cast<uint32_t *>(stage);
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it)
+      if (dig[it] < BINS) vstage[pos[it]] = val[it];
+    __syncthreads();
+    for (int p = threadIdx.x; p < count; p += kSortBlock) {
+      const int d = stage_d[p];
+      vout[gbase[d] + (p - tile_prefix[d])] = vstage[p];
+    }
+  }
+}
+
+template <typename K, int BITS, bool VALS>
+cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
+                      int begin_bit, int end_bit, void *workspace, int *which,
+                      int64_t *launches) {
+  constexpr int BINS = 1 << BITS;
+  constexpr int TILE = TileShape<K>::tile;
+  *which = 0;
+  if (n <= 1) return cudaSuccess;
+  const int64_t ntiles = num_tiles(n, TILE);
+  uint32_t *hist = static_cast<uint32_t *>(workspace);
+  uint32_t *totals = hist + int64_t(BINS) * ntiles;
+  int cur = 0;
+  for (int shift = begin_bit; shift < end_bit; shift += BITS) {
+    upsweep_kernel<K, BITS><<<unsigned(ntiles), kSortBlock, 0, s>>>(kbuf[cur], n, shift,
+                                                                     hist, ntiles);
+    scan_rows_kernel<<<BINS, kSortBlock, 0, s>>>(hist, ntiles, totals);
+    scan_totals_kernel<BINS><<<1, kSortBlock, 0, s>>>(totals);
+    downsweep_kernel<K, BITS, VALS><<<unsigned(ntiles), kSortBlock, 0, s>>>(
+        kbuf[cur], kbuf[cur ^ 1], VALS ? vbuf[cur] : nullptr,
+        VALS ? vbuf[cur ^ 1] : nullptr, n, shift, hist, totals, ntiles);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    if (launches) *launches += 4;
+    cur ^= 1;
+  }
+  *which = cur;
+  return cudaSuccess;
+}
+
+}  // namespace
+
+size_t radix_workspace_bytes(int64_t n, int key_bytes, int bits) {
+  const int tile = key_bytes == 4 ? TileShape<uint32_t>::tile : TileShape<unsigned long long>::tile;
+  const int64_t ntiles = num_tiles(n > 0 ? n : 1, tile);
+  return sizeof(uint32_t) * (size_t(1 << bits) * ntiles + (1 << bits)) + 256;
+}
+
+cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
+                           int64_t n, int bits, void *workspace, int *which,
+                           int64_t *launches) {
+  if (bits == 4)
+    return sort_impl<uint32_t, 4, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches);
+  return sort_impl<uint32_t, 8, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches);
+}
+
+cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2], int64_t n,
+                           int begin_bit, int end_bit, void *workspace, int *which,
+                           int64_t *launches) {
+  return sort_impl<unsigned long long, 8, false>(s, kbuf, nullptr, n, begin_bit, end_bit,
+                                                 workspace, which, launches);
+}
+
+}  // namespace stq

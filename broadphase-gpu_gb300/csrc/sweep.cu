@@ -1,0 +1,333 @@
+// sweep.cu - the sweep-and-tiniest-queue pass, pair compaction, the
+// overflow prefix selection and the all-pairs checker.
+//
+// Reference: twostage_queue (src/sweep.cu:226-279) with its shared Queue
+// (src/queue.cuh:9-38, src/queue.cu:75-115), does_collide / covertex /
+// is_valid_pair (src/collision.cu:38-48, src/aabb.cu:33-40) and add_overlap
+// (src/collision.cu:50-74).
+//
+// GB300 design. Each warp owns a shared-memory ring of pending start boxes
+// (the "tiniest queue"). The warp is split into lane groups of G lanes; a
+// group takes one start box k from the ring and walks its x-run
+// j = k+1, k+2, ... G candidates per step, until the first j whose min
+// exceeds k's max (a NaN sentinel ends every run). A group that finishes
+// takes the next pending box, so a long run never stalls the other groups.
+// Refill, hand-out and pair output use __ballot_sync/__popc compaction: no
+// shared-memory atomics, and one global atomic per warp step that emits.
+#include "stq_device.cuh"
+#include "stq_internal.h"
+
+namespace stq {
+
+namespace {
+
+template <int G, int Q, int BLOCK, bool COUNT>
+__global__ void __launch_bounds__(BLOCK)
+stq_sweep_kernel(const SweepParams p) {
+  static_assert(32 % G == 0, "lane group must divide the warp");
+  static_assert((Q & (Q - 1)) == 0 && Q >= 32, "queue depth: power of two >= 32");
+  constexpr int E = 32 / G;  // lane groups per warp
+  __shared__ int ring[BLOCK / 32][Q];
+
+  const int lane = threadIdx.x & 31;
+  const int gl = lane % G;              // lane within group
+  const int grp = lane / G;             // group within warp
+  const unsigned grp_mask = G == 32 ? kFullMask : (((1u << G) - 1u) << (grp * G));
+  const unsigned upto_me = grp_mask & (lane == 31 ? kFullMask : ((2u << lane) - 1u));
+  const unsigned leaders_below = (grp * G) == 0 ? 0u : ((1u << (grp * G)) - 1u);
+  int *q = ring[threadIdx.x >> 5];
+
+  // warp-uniform queue and work state
+  int qhead = 0, qsize = 0;
+  int next_k = 0, chunk_end = 0;
+  bool more = true;
+  // lane-group state (identical in the G lanes of a group)
+  int k = -1, j0 = 0, acc = 0;
+  float kmax = 0.f;
+  float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
+  int4 kv = make_int4(0, 0, 0, 0);
+  const int span = p.end - p.begin;
+
+  while (true) {
+    // 1. Refill the ring with start boxes that have at least one candidate.
+    while (qsize < E && more) {
+      if (next_k >= chunk_end) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(p.work, p.chunk);
+        c = __shfl_sync(kFullMask, c, 0);
+        if (c >= span) {
+          more = false;
+          break;
+        }
+        next_k = p.begin + c;
+        chunk_end = min(next_k + p.chunk, p.end);
+      }
+      const int take = min(32, min(Q - qsize, chunk_end - next_k));
+      const int kk = next_k + lane;
+      bool push = false;
+      if (lane < take) push = p.sx[kk + 1].x <= p.sx[kk].y;
+      const unsigned m = __ballot_sync(kFullMask, push);
+      if (push) q[(qhead + qsize + __popc(m & lanemask_lt())) & (Q - 1)] = kk;
+      qsize += __popc(m);
+      next_k += take;
+    }
+    __syncwarp();
+    // 2. Idle groups take pending start boxes, in ring order.
+    const bool idle = k < 0;
+    const unsigned needm = __ballot_sync(kFullMask, idle && gl == 0);
+    const int ntake = min(__popc(needm), qsize);
+    if (idle) {
+      const int r = __popc(needm & leaders_below);
+      if (r < ntake) {
+        k = q[(qhead + r) & (Q - 1)];
+        j0 = k + 1;
+        kmax = p.sx[k].y;
+        kb = p.syz[k];
+        kv = p.sv[k];
+        acc = 0;
+      }
+    }
+    qhead = (qhead + ntake) & (Q - 1);
+    qsize -= ntake;
+    __syncwarp();
+    const bool active = k >= 0;
+    if (__ballot_sync(kFullMask, active) == 0) {
+      if (!more && qsize == 0) break;
+      continue;
+    }
+    // 3. Test G consecutive candidates per group. Valid lanes form the
+    //    prefix of the group before the first x-test failure.
+    const int j = j0 + gl;
+    const bool xok = active && p.sx[j].x <= kmax;
+    const unsigned failm = __ballot_sync(kFullMask, active && !xok);
+    const bool valid = active && (failm & upto_me) == 0;
+    bool hit = false;
+    int lo_id = 0, hi_id = 0;
+    if (valid) {
+      const float4 b = p.syz[j];
+      const int4 bv = p.sv[j];
+      hit = overlap_bc(kb, b) && valid_pair(kv, bv) && !covertex(kv, bv);
+      lo_id = min(kv.w, bv.w);
+      hi_id = max(kv.w, bv.w);
+    }
+    // 4. Emit: one global atomic per warp step.
+    const unsigned hm = __ballot_sync(kFullMask, hit);
+    if (COUNT) {
+      acc += __popc(hm & grp_mask);
+    } else if (hm) {
+      unsigned long long base = 0;
+      if (lane == 0) base = atomicAdd(p.count, (unsigned long long)__popc(hm));
+      base = __shfl_sync(kFullMask, base, 0);
+      if (hit) {
+        const unsigned long long idx = base + __popc(hm & lanemask_lt());
+        if (idx < (unsigned long long)p.capacity)
+          reinterpret_cast<int2 *>(p.pairs)[idx] = make_int2(lo_id, hi_id);
+      }
+    }
+    // 5. A group whose G lanes all passed continues; otherwise its run ended.
+    const unsigned vm = __ballot_sync(kFullMask, valid);
+    if (active) {
+      if ((vm & grp_mask) == grp_mask) {
+        j0 += G;
+      } else {
+        if (COUNT && gl == 0) p.box_counts[k - p.begin] = acc;
+        k = -1;
+      }
+    }
+  }
+}
+
+template <int G, int Q, int BLOCK>
+cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, bool count_mode, int num_sms) {
+  int per_sm = 0;
+  auto kern = count_mode ? stq_sweep_kernel<G, Q, BLOCK, true> : stq_sweep_kernel<G, Q, BLOCK, false>;
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, 0);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) per_sm = 1;
+  // persistent grid: all resident blocks, capped by the available work
+  const int64_t warps_needed = (int64_t(p.end - p.begin) + p.chunk - 1) / p.chunk;
+  int64_t blocks = int64_t(num_sms) * per_sm;
+  const int64_t max_useful = (warps_needed + BLOCK / 32 - 1) / (BLOCK / 32);
+  if (blocks > max_useful) blocks = max_useful;
+  if (blocks < 1) blocks = 1;
+  kern<<<unsigned(blocks), BLOCK, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+template <int G, int Q>
+cudaError_t launch_gq(cudaStream_t s, const SweepParams &p, int block, bool cm, int sms) {
+  switch (block) {
+    case 128: return launch_gqb<G, Q, 128>(s, p, cm, sms);
+    case 512: return launch_gqb<G, Q, 512>(s, p, cm, sms);
+    default: return launch_gqb<G, Q, 256>(s, p, cm, sms);
+  }
+}
+
+template <int G>
+cudaError_t launch_g(cudaStream_t s, const SweepParams &p, const SweepTuning &t, bool cm, int sms) {
+  switch (t.queue) {
+    case 32: return launch_gq<G, 32>(s, p, t.block, cm, sms);
+    case 128: return launch_gq<G, 128>(s, p, t.block, cm, sms);
+    default: return launch_gq<G, 64>(s, p, t.block, cm, sms);
+  }
+}
+
+// ---- overflow: longest prefix of start boxes whose pairs fit ------------------
+constexpr int kScanBlock = 256;
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kScanBlock * kScanItems;
+
+__global__ void __launch_bounds__(kScanBlock)
+tile_sums_kernel(const int32_t *__restrict__ c, int64_t m, long long *__restrict__ sums) {
+  const int64_t base = int64_t(blockIdx.x) * kScanTile;
+  long long s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    const int64_t idx = base + int64_t(i) * kScanBlock + threadIdx.x;
+    if (idx < m) s += c[idx];
+  }
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(kFullMask, s, o);
+  __shared__ long long red[kScanBlock / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    long long t = 0;
+    for (int w = 0; w < kScanBlock / 32; ++w) t += red[w];
+    sums[blockIdx.x] = t;
+  }
+}
+
+// Single thread: exclusive scan of the tile sums and the last tile whose
+// start is within capacity. Tiles are few (m / 2048).
+__global__ void tile_select_kernel(long long *__restrict__ sums, int64_t ntiles,
+                                   long long capacity, long long *__restrict__ sel) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  long long run = 0;
+  int64_t last = 0;
+  for (int64_t t = 0; t < ntiles; ++t) {
+    const long long v = sums[t];
+    sums[t] = run;
+    if (run <= capacity) last = t;
+    run += v;
+  }
+  sel[0] = last;
+}
+
+// Within the selected tile: the longest prefix whose inclusive sum fits.
+__global__ void __launch_bounds__(kScanBlock)
+prefix_in_tile_kernel(const int32_t *__restrict__ c, int64_t m,
+                      const long long *__restrict__ sums, const long long *__restrict__ sel,
+                      long long capacity, DevScalars *scalars) {
+  const int64_t t = sel[0];
+  const int64_t base = t * kScanTile;
+  if (threadIdx.x == 0) {
+    long long run = sums[t];
+    int64_t prefix = base;
+    for (int64_t i = base; i < m && i < base + kScanTile; ++i) {
+      run += c[i];
+      if (run > capacity) break;
+      prefix = i + 1;
+    }
+    scalars->prefix = prefix;
+  }
+}
+
+// ---- all-pairs checker (get_collision_pairs, src/collision.cu:91-154) ---------
+constexpr int kBruteTile = 128;
+
+__global__ void __launch_bounds__(kBruteTile)
+brute_force_kernel(const stq_aabb *__restrict__ boxes, int64_t n,
+                   stq_pair *__restrict__ pairs, long long capacity,
+                   unsigned long long *count) {
+  __shared__ stq_aabb tile[kBruteTile];
+  const int64_t i = int64_t(blockIdx.x) * kBruteTile + threadIdx.x;
+  stq_aabb a;
+  if (i < n) a = boxes[i];
+  for (int64_t t0 = int64_t(blockIdx.y) * kBruteTile; t0 < n; t0 += int64_t(gridDim.y) * kBruteTile) {
+    __syncthreads();
+    if (t0 + threadIdx.x < n) tile[threadIdx.x] = boxes[t0 + threadIdx.x];
+    __syncthreads();
+    if (i >= n) continue;
+    for (int q = 0; q < kBruteTile && t0 + q < n; ++q) {
+      const int64_t jj = t0 + q;
+      if (jj <= i) continue;
+      const stq_aabb &b = tile[q];
+      bool ov = true;
+      for (int k = 0; k < 3; ++k) ov = ov && a.max[k] >= b.min[k] && a.min[k] <= b.max[k];
+      const int4 av = make_int4(a.vertex_ids[0], a.vertex_ids[1], a.vertex_ids[2], a.id);
+      const int4 bv = make_int4(b.vertex_ids[0], b.vertex_ids[1], b.vertex_ids[2], b.id);
+      if (ov && valid_pair(av, bv) && !covertex(av, bv)) {
+        const unsigned long long idx = atomicAdd(count, 1ull);
+        if (idx < (unsigned long long)capacity)
+          reinterpret_cast<int2 *>(pairs)[idx] = make_int2(min(a.id, b.id), max(a.id, b.id));
+      }
+    }
+  }
+}
+
+__global__ void pairs_keys_kernel(stq_pair *pairs, int64_t n, unsigned long long *keys,
+                                  bool to_keys) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    if (to_keys) {
+      keys[i] = (static_cast<unsigned long long>(uint32_t(pairs[i].first)) << 32) |
+                uint32_t(pairs[i].second);
+    } else {
+      pairs[i].first = int32_t(keys[i] >> 32);
+      pairs[i].second = int32_t(keys[i] & 0xffffffffu);
+    }
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
+                         bool count_mode, int num_sms) {
+  if (p.end <= p.begin) return cudaSuccess;
+  switch (t.lanes) {
+    case 1: return launch_g<1>(s, p, t, count_mode, num_sms);
+    case 2: return launch_g<2>(s, p, t, count_mode, num_sms);
+    case 4: return launch_g<4>(s, p, t, count_mode, num_sms);
+    case 16: return launch_g<16>(s, p, t, count_mode, num_sms);
+    case 32: return launch_g<32>(s, p, t, count_mode, num_sms);
+    default: return launch_g<8>(s, p, t, count_mode, num_sms);
+  }
+}
+
+size_t prefix_workspace_bytes(int64_t m) {
+  const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
+  return sizeof(long long) * (ntiles + 2);
+}
+
+cudaError_t launch_prefix_select(cudaStream_t s, const int32_t *box_counts, int64_t m,
+                                 long long capacity, void *workspace, DevScalars *scalars,
+                                 int64_t *launches) {
+  const int64_t ntiles = (m + kScanTile - 1) / kScanTile;
+  long long *sums = static_cast<long long *>(workspace);
+  long long *sel = sums + ntiles + 1;
+  tile_sums_kernel<<<unsigned(ntiles), kScanBlock, 0, s>>>(box_counts, m, sums);
+  tile_select_kernel<<<1, 32, 0, s>>>(sums, ntiles, capacity, sel);
+  prefix_in_tile_kernel<<<1, kScanBlock, 0, s>>>(box_counts, m, sums, sel, capacity, scalars);
+  if (launches) *launches += 3;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brute_force(cudaStream_t s, const stq_aabb *boxes, int64_t n,
+                               stq_pair *pairs, long long capacity,
+                               unsigned long long *count) {
+  if (n < 2) return cudaSuccess;
+  const int64_t tiles = (n + kBruteTile - 1) / kBruteTile;
+  dim3 grid(unsigned(tiles), unsigned(tiles < 64 ? tiles : 64));
+  brute_force_kernel<<<grid, kBruteTile, 0, s>>>(boxes, n, pairs, capacity, count);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_to_keys(cudaStream_t s, const stq_pair *pairs, int64_t n,
+                                 unsigned long long *keys, bool to_keys) {
+  if (n == 0) return cudaSuccess;
+  int64_t g = (n + 255) / 256;
+  if (g > 152 * 16) g = 152 * 16;
+  pairs_keys_kernel<<<unsigned(g), 256, 0, s>>>(const_cast<stq_pair *>(pairs), n, keys, to_keys);
+  return cudaGetLastError();
+}
+
+}  // namespace stq

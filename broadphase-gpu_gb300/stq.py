@@ -1,0 +1,303 @@
+"""Python host binding of the STQ broad phase C ABI (include/stq_abi.h).
+
+A thin ctypes layer: every compute call goes through libstq_gb300.so. PyTorch
+is used only to hold device memory and to name the CUDA stream. There is no
+CPU fallback: loading fails loudly if the native library is missing.
+
+Reference interfaces mirrored (Ahdhn/broadphase-gpu):
+  Context.build_boxes   stq::gpu::constructBoxes          src/io.cuh:9-13
+  Context.select_axis   calc_mean / calc_variance          src/sweep.cu:93-123
+  Context.sweep         stq::gpu::run_sweep_sharedqueue   src/simulation.cuh:22-27
+  Context.sweep_host    the same with host boxes and host pairs
+                        (KEEP_CPU_OVERLAPS, src/simulation.cu:763-780)
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = PKG / "_build" / "libstq_gb300.so"
+SCENES_PATH = PKG / "_build" / "libstq_scenes.so"
+
+# stq_aabb: 44 bytes, the reference's stq::gpu::Aabb (src/aabb.cuh:15-43)
+AABB_DTYPE = np.dtype([
+    ("id", "<i4"), ("min", "<f4", (3,)), ("max", "<f4", (3,)),
+    ("vertex_ids", "<i4", (3,)), ("ref_id", "<i4"),
+])
+assert AABB_DTYPE.itemsize == 44
+
+STQ_OK = 0
+STQ_OVERFLOW = 1
+STQ_ERR_INVALID_ARG = -1
+STQ_ERR_INVALID_INPUT = -2
+STQ_ERR_CUDA = -3
+STQ_ERR_NO_MEMORY = -4
+STQ_ERR_CAPACITY = -5
+STQ_ERR_TIMEOUT = -6
+STQ_ERR_NOT_PREPARED = -7
+
+AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
+OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS = 1, 2, 3, 4, 5
+
+_c_i64p = ctypes.POINTER(ctypes.c_int64)
+_vp = ctypes.c_void_p
+
+# name -> (restype, argtypes): the full exported surface of include/stq_abi.h
+ABI_SIGNATURES = {
+    "stq_abi_version": (ctypes.c_int, []),
+    "stq_status_string": (ctypes.c_char_p, [ctypes.c_int]),
+    "stq_context_create": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.POINTER(_vp)]),
+    "stq_context_destroy": (None, [_vp]),
+    "stq_context_set_stream": (ctypes.c_int, [_vp, _vp]),
+    "stq_context_set_option": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int64]),
+    "stq_context_get_option": (ctypes.c_int64, [_vp, ctypes.c_int]),
+    "stq_context_last_error": (ctypes.c_char_p, [_vp]),
+    "stq_context_launch_count": (ctypes.c_int64, [_vp]),
+    "stq_build_boxes": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64,
+                                       _vp, ctypes.c_int64, ctypes.c_float, _vp]),
+    "stq_select_axis": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
+    "stq_prepare": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int]),
+    "stq_sweep_prepared": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64,
+                                          _c_i64p, _c_i64p, _c_i64p]),
+    "stq_sweep": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
+                                 ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p, _c_i64p, _c_i64p]),
+    "stq_sweep_host": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, _vp, ctypes.c_int64,
+                                      _c_i64p, _c_i64p]),
+    "stq_sort_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
+    "stq_brute_force": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p]),
+}
+
+_lib = None
+_scenes = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads libstq_gb300.so (built in-tree); raises if it is missing."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"native STQ library missing: {LIB_PATH} (run build())")
+        lib = ctypes.CDLL(str(LIB_PATH))
+        for name, (res, args) in ABI_SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def load_scenes() -> ctypes.CDLL:
+    global _scenes
+    if _scenes is None:
+        if not SCENES_PATH.exists():
+            raise RuntimeError(f"scene library missing: {SCENES_PATH} (run build())")
+        _scenes = ctypes.CDLL(str(SCENES_PATH))
+    return _scenes
+
+
+class STQError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"STQ status {status}: {message}")
+        self.status = status
+
+
+@dataclass
+class SweepResult:
+    status: int
+    count: int
+    next_start: int
+    total: int
+
+
+def _ptr(t) -> int | None:
+    if t is None:
+        return None
+    if isinstance(t, np.ndarray):
+        return t.ctypes.data
+    return t.data_ptr()
+
+
+class Context:
+    """One STQ context on one device and one stream (stq_context*)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self.lib = load_library()
+        self._h = _vp()
+        st = self.lib.stq_context_create(device, stream, ctypes.byref(self._h))
+        if st != STQ_OK:
+            raise STQError(st, "context creation failed")
+        self.device = device
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.stq_context_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- helpers --------------------------------------------------------------
+    def _check(self, st: int, allow=(STQ_OK,)) -> int:
+        if st not in allow:
+            msg = self.lib.stq_context_last_error(self._h)
+            raise STQError(st, (msg or b"").decode())
+        return st
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_stream(self, stream: int | None) -> None:
+        self._check(self.lib.stq_context_set_stream(self._h, stream))
+
+    def set_option(self, option: int, value: int) -> None:
+        self._check(self.lib.stq_context_set_option(self._h, option, value))
+
+    def get_option(self, option: int) -> int:
+        return int(self.lib.stq_context_get_option(self._h, option))
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.stq_context_launch_count(self._h))
+
+    # -- pipeline -------------------------------------------------------------
+    def build_boxes(self, V0, V1, E, F, out, inflation_radius: float = 0.0) -> None:
+        """Swept boxes from device tensors V0/V1 [nV,3] f64, E [nE,2] i32, F [nF,3] i32
+        into `out` (device buffer of (nV+nE+nF)*44 bytes)."""
+        nV, nE, nF = V0.shape[0], E.shape[0], F.shape[0]
+        self._check(self.lib.stq_build_boxes(self._h, _ptr(V0), _ptr(V1), nV, _ptr(E), nE,
+                                             _ptr(F), nF, float(inflation_radius), _ptr(out)))
+
+    def select_axis(self, boxes, n: int) -> int:
+        a = ctypes.c_int(-1)
+        self._check(self.lib.stq_select_axis(self._h, _ptr(boxes), n, ctypes.byref(a)))
+        return a.value
+
+    def prepare(self, boxes, n: int, axis: int = AXIS_X) -> None:
+        self._check(self.lib.stq_prepare(self._h, _ptr(boxes), n, axis))
+
+    def sweep_prepared(self, pairs, capacity: int, start: int = 0, max_start: int = 0) -> SweepResult:
+        c, nx, tot = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_sweep_prepared(self._h, start, max_start, _ptr(pairs), capacity,
+                                         ctypes.byref(c), ctypes.byref(nx), ctypes.byref(tot))
+        self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
+        return SweepResult(st, c.value, nx.value, tot.value)
+
+    def sweep(self, boxes, n: int, pairs, capacity: int, axis: int = AXIS_X,
+              start: int = 0, max_start: int = 0) -> SweepResult:
+        c, nx, tot = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_sweep(self._h, _ptr(boxes), n, axis, start, max_start, _ptr(pairs),
+                                capacity, ctypes.byref(c), ctypes.byref(nx), ctypes.byref(tot))
+        self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
+        return SweepResult(st, c.value, nx.value, tot.value)
+
+    def sweep_host(self, boxes: np.ndarray, pairs: np.ndarray, axis: int = AXIS_X) -> SweepResult:
+        """Host boxes (AABB_DTYPE) in, host pairs (int32 [cap, 2]) out."""
+        assert boxes.dtype == AABB_DTYPE and boxes.flags.c_contiguous
+        assert pairs.dtype == np.int32 and pairs.flags.c_contiguous
+        c, tot = ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_sweep_host(self._h, boxes.ctypes.data, boxes.shape[0], axis,
+                                     pairs.ctypes.data, pairs.shape[0], ctypes.byref(c),
+                                     ctypes.byref(tot))
+        self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
+        return SweepResult(st, c.value, boxes.shape[0], tot.value)
+
+    def sort_pairs(self, pairs, count: int) -> None:
+        self._check(self.lib.stq_sort_pairs(self._h, _ptr(pairs), count))
+
+    def brute_force(self, boxes, n: int, pairs, capacity: int) -> int:
+        c = ctypes.c_int64()
+        self._check(self.lib.stq_brute_force(self._h, _ptr(boxes), n, _ptr(pairs), capacity,
+                                             ctypes.byref(c)), allow=(STQ_OK, STQ_OVERFLOW))
+        return c.value
+
+
+# ---- synthetic scenes (libstq_scenes.so) ----------------------------------------
+@dataclass
+class Mesh:
+    V0: np.ndarray  # [nV, 3] f64
+    V1: np.ndarray
+    E: np.ndarray   # [nE, 2] i32
+    F: np.ndarray   # [nF, 3] i32
+
+    @property
+    def num_boxes(self) -> int:
+        return self.V0.shape[0] + self.E.shape[0] + self.F.shape[0]
+
+
+def grid_counts(g: int) -> tuple[int, int, int]:
+    lib = load_scenes()
+    nv, ne, nf = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    lib.stq_grid_counts(ctypes.c_int(g), ctypes.byref(nv), ctypes.byref(ne), ctypes.byref(nf))
+    return nv.value, ne.value, nf.value
+
+
+def _alloc_mesh(sheets: int, g: int) -> Mesh:
+    nv, ne, nf = grid_counts(g)
+    return Mesh(np.empty((sheets * nv, 3)), np.empty((sheets * nv, 3)),
+                np.empty((sheets * ne, 2), np.int32), np.empty((sheets * nf, 3), np.int32))
+
+
+def cloth_pair(g: int = 200, z_offset: float = 0.01, angle_deg: float = 10.0,
+               sigma: float = 0.003, seed: int = 0) -> Mesh:
+    """Two g x g cloth sheets (the single-scene and batched cloth-pair workloads)."""
+    lib = load_scenes()
+    m = _alloc_mesh(2, g)
+    lib.stq_scene_cloth_pair(ctypes.c_int(g), ctypes.c_double(z_offset), ctypes.c_double(angle_deg),
+                             ctypes.c_double(sigma), ctypes.c_uint64(seed),
+                             m.V0.ctypes.data_as(_vp), m.V1.ctypes.data_as(_vp),
+                             m.E.ctypes.data_as(_vp), m.F.ctypes.data_as(_vp))
+    return m
+
+
+def crumpled_sheets(sheets: int = 16, g: int = 250, amp: float = 0.05, sigma: float = 0.005,
+                    seed: int = 1) -> Mesh:
+    """`sheets` interpenetrating crumpled g x g sheets (the large single-scene workload)."""
+    lib = load_scenes()
+    m = _alloc_mesh(sheets, g)
+    lib.stq_scene_crumpled(ctypes.c_int(sheets), ctypes.c_int(g), ctypes.c_double(amp),
+                           ctypes.c_double(sigma), ctypes.c_uint64(seed),
+                           m.V0.ctypes.data_as(_vp), m.V1.ctypes.data_as(_vp),
+                           m.E.ctypes.data_as(_vp), m.F.ctypes.data_as(_vp))
+    return m
+
+
+def random_boxes(n: int, sliver_frac: float = 0.05, seed: int = 3) -> np.ndarray:
+    """n random boxes with lognormal extents and 200x slivers (the skewed workload)."""
+    lib = load_scenes()
+    out = np.empty(n, AABB_DTYPE)
+    lib.stq_scene_random_boxes(ctypes.c_int64(n), ctypes.c_double(sliver_frac),
+                               ctypes.c_uint64(seed), out.ctypes.data_as(_vp))
+    return out
+
+
+def cloth_pair_grid_for(boxes: int) -> int:
+    lib = load_scenes()
+    lib.stq_cloth_pair_grid_for.restype = ctypes.c_int
+    return int(lib.stq_cloth_pair_grid_for(ctypes.c_int64(boxes)))
+
+
+def scene_step(mesh: Mesh, sigma: float, seed: int) -> None:
+    """One serving time step: V0 <- V1, V1 <- V1 + N(0, sigma^2)."""
+    lib = load_scenes()
+    lib.stq_scene_step(ctypes.c_int64(mesh.V0.shape[0]), ctypes.c_double(sigma),
+                       ctypes.c_uint64(seed), mesh.V0.ctypes.data_as(_vp), mesh.V1.ctypes.data_as(_vp))
+
+
+def splitmix64(x: int) -> int:
+    lib = load_scenes()
+    lib.stq_splitmix64.restype = ctypes.c_uint64
+    return int(lib.stq_splitmix64(ctypes.c_uint64(x)))

@@ -1,0 +1,160 @@
+/*
+ * stq_abi.h - C ABI of the GB300 sweep-and-tiniest-queue (STQ) broad phase.
+ *
+ * Plain C: pointers, sizes and status codes only. Every pointer argument
+ * named d_* is a device pointer on the context's device; h_* is host memory.
+ * All work is enqueued on the context's stream. A call that returns a count
+ * or a cursor to the host synchronises that stream before returning.
+ *
+ * Reference interfaces replaced (paths are within Ahdhn/broadphase-gpu):
+ *   stq_aabb             <- stq::gpu::Aabb                src/aabb.cuh:15-43
+ *   stq_build_boxes      <- stq::gpu::constructBoxes      src/io.cuh:9-13
+ *                           (addVertices/addEdges/addFaces src/aabb.cu:193-304,
+ *                            CPU twin src/cpu/aabb.cpp:7-95)
+ *   stq_select_axis      <- calc_mean / calc_variance     src/sweep.cu:93-123
+ *                           (axis choice, src/simulation.cu:594-637)
+ *   stq_prepare          <- create_ds + thrust::sort_by_key
+ *                           src/sweep.cu:125-161, src/simulation.cu:641-649
+ *   stq_sweep_prepared   <- twostage_queue + add_overlap + the overflow loop
+ *                           src/sweep.cu:226-279, src/collision.cu:50-74,
+ *                           src/simulation.cu:690-747
+ *   stq_sweep            <- stq::gpu::run_sweep_sharedqueue (device part)
+ *                           src/simulation.cuh:22-27, src/simulation.cu:555-782
+ *   stq_sweep_host       <- the same call with host boxes in and host pairs
+ *                           out (H2D at simulation.cu:580, KEEP_CPU_OVERLAPS
+ *                           copy-back at simulation.cu:763-780)
+ *   stq_brute_force      <- get_collision_pairs (all-pairs checker)
+ *                           src/collision.cu:91-154
+ */
+#ifndef STQ_ABI_H
+#define STQ_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define STQ_ABI_VERSION 1
+
+/* Status codes. Negative values are errors; STQ_OVERFLOW is a partial result. */
+typedef enum stq_status {
+  STQ_OK = 0,
+  /* The pairs of the requested start-box range did not fit in the caller's
+   * buffer. The call wrote every pair of the longest prefix of start boxes
+   * that fits, set *next_start to the first start box not yet swept and
+   * *total to the pair count of the whole requested range. Call again from
+   * *next_start (the reference's tidstart resume cursor). */
+  STQ_OVERFLOW = 1,
+  STQ_ERR_INVALID_ARG = -1,   /* null pointer, negative size, bad option     */
+  STQ_ERR_INVALID_INPUT = -2, /* a box bound is NaN, or an index is out of range */
+  STQ_ERR_CUDA = -3,          /* a CUDA runtime call failed (see last_error)  */
+  STQ_ERR_NO_MEMORY = -4,     /* device or host allocation failed            */
+  STQ_ERR_CAPACITY = -5,      /* one start box alone has more pairs than the buffer holds */
+  STQ_ERR_TIMEOUT = -6,       /* a bounded device-side wait expired          */
+  STQ_ERR_NOT_PREPARED = -7   /* stq_sweep_prepared without a prepared scene */
+} stq_status;
+
+/* Swept box, 44 bytes, field for field the reference's stq::gpu::Aabb
+ * (src/aabb.cuh:15-43, Scalar = float): id, min, max, vertexIds, ref_id.
+ * Box type is encoded in the signs of vertexIds (src/aabb.cu:12-40):
+ *   vertex: {v, -v-1, -v-1}, edge: {e0, e1, -e0-1}, face: {f0, f1, f2}. */
+typedef struct stq_aabb {
+  int32_t id;
+  float min[3];
+  float max[3];
+  int32_t vertex_ids[3];
+  int32_t ref_id;
+} stq_aabb;
+
+/* One overlap, written as (smaller id, larger id). Layout of CUDA int2. */
+typedef struct stq_pair {
+  int32_t first;
+  int32_t second;
+} stq_pair;
+
+/* Sweep axis. STQ_AXIS_AUTO picks the axis of largest box-corner variance. */
+enum { STQ_AXIS_AUTO = -1, STQ_AXIS_X = 0, STQ_AXIS_Y = 1, STQ_AXIS_Z = 2 };
+
+/* Tuning knobs for stq_context_set_option (0 restores the automatic choice). */
+typedef enum stq_option {
+  STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1,2,4,8,16,32 */
+  STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 32, 64 or 128           */
+  STQ_OPT_BLOCK_SIZE = 3,      /* sweep block size: 128, 256 or 512               */
+  STQ_OPT_CELLS = 4,           /* y/z cell grid side (1 = no cells, 0 = automatic) */
+  STQ_OPT_RADIX_BITS = 5       /* radix digit width: 4 or 8                       */
+} stq_option;
+
+typedef struct stq_context stq_context;
+
+int stq_abi_version(void);
+const char *stq_status_string(int status);
+
+/* Creates a context bound to `device` and `stream` (a cudaStream_t; NULL =
+ * the legacy default stream). The context owns a grow-only device arena. */
+int stq_context_create(int device, void *stream, stq_context **out);
+void stq_context_destroy(stq_context *ctx);
+int stq_context_set_stream(stq_context *ctx, void *stream);
+int stq_context_set_option(stq_context *ctx, int option, int64_t value);
+int64_t stq_context_get_option(const stq_context *ctx, int option);
+const char *stq_context_last_error(const stq_context *ctx);
+/* Kernel launches this context issued since it was created. */
+int64_t stq_context_launch_count(const stq_context *ctx);
+
+/* Swept boxes from vertex trajectories. d_V0/d_V1 are row-major [nV x 3]
+ * fp64 positions at t0 and t1, d_E [nE x 2] and d_F [nF x 3] int32 vertex
+ * indices. Writes nV + nE + nF boxes in id order (vertices, edges, faces):
+ * per coordinate, min over the trajectory points in fp64, rounded to float,
+ * moved one ulp outward, then widened by nextafter_up(inflation_radius). */
+int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1,
+                    int64_t nV, const int32_t *d_E, int64_t nE,
+                    const int32_t *d_F, int64_t nF, float inflation_radius,
+                    stq_aabb *d_boxes);
+
+/* Axis of largest variance of the box corners (0, 1 or 2). */
+int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
+                    int *axis_out);
+
+/* Sorts the boxes along `axis` into the context's sorted scene (keys,
+ * bounds, vertex ids). The boxes buffer may be reused after return. */
+int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
+                int axis);
+
+/* Sweeps start boxes [start, start + max_start) of the prepared scene in
+ * sorted order (max_start <= 0 means all). Every overlapping pair whose
+ * earlier box lies in that range is written once to d_pairs as
+ * (smaller id, larger id), in no particular order. *count = pairs written,
+ * *next_start = first start box not swept, *total (may be NULL) = pairs of
+ * the whole range. Returns STQ_OK or STQ_OVERFLOW (see above). */
+int stq_sweep_prepared(stq_context *ctx, int64_t start, int64_t max_start,
+                       stq_pair *d_pairs, int64_t capacity, int64_t *count,
+                       int64_t *next_start, int64_t *total);
+
+/* stq_prepare + stq_sweep_prepared in one call. */
+int stq_sweep(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis,
+              int64_t start, int64_t max_start, stq_pair *d_pairs,
+              int64_t capacity, int64_t *count, int64_t *next_start,
+              int64_t *total);
+
+/* End-to-end call on host memory: copies h_boxes to the device, sweeps all
+ * start boxes, copies the pairs back to h_pairs (capacity entries). Same
+ * return codes as stq_sweep; on STQ_OVERFLOW h_pairs holds the prefix. */
+int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n,
+                   int axis, stq_pair *h_pairs, int64_t capacity,
+                   int64_t *count, int64_t *total);
+
+/* Sorts d_pairs[0..count) lexicographically on the device (deterministic
+ * output order for callers that need one). */
+int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count);
+
+/* All-pairs checker, O(n^2): same filter and output form as the sweep.
+ * Meant for small n (cross-checks). */
+int stq_brute_force(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
+                    stq_pair *d_pairs, int64_t capacity, int64_t *count);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* STQ_ABI_H */

@@ -1,0 +1,321 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle and the
+golden fixtures. Integer/index results and float bounds are bit-exact."""
+import numpy as np
+import pytest
+
+from conftest import decode_boxes, decode_mesh, expected_pairs
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(arr, cuda):
+    import torch
+
+    return torch.from_numpy(np.ascontiguousarray(arr)).to(cuda)
+
+
+def boxes_dev(boxes, cuda):
+    import torch
+
+    flat = np.ascontiguousarray(boxes).view(np.int32).reshape(-1, 11)
+    return torch.from_numpy(flat.copy()).to(cuda)
+
+
+def build_dev(ctx, mesh_arrays, cuda, r=0.0):
+    import torch
+
+    V0, V1, E, F = mesh_arrays
+    n = V0.shape[0] + E.shape[0] + F.shape[0]
+    out = torch.empty((max(n, 1), 11), dtype=torch.int32, device=cuda)
+    ctx.build_boxes(dev(V0, cuda), dev(V1, cuda), dev(E.reshape(-1, 2), cuda),
+                    dev(F.reshape(-1, 3), cuda), out, r)
+    return out, n
+
+
+def to_host_boxes(t, n, stq):
+    return t[:n].cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
+
+
+def sweep_pairs(ctx, stq, oracle, bdev, n, cuda, axis=0, cap=None):
+    import torch
+
+    cap = cap if cap is not None else max(16, 64 * n)
+    pairs = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=cuda)
+    r = ctx.sweep(bdev, n, pairs, cap, axis=axis)
+    assert r.status == stq.STQ_OK, r
+    assert r.count == r.total and r.next_start == n
+    raw = pairs[: r.count].cpu().numpy()
+    assert np.all(raw[:, 0] < raw[:, 1]) if len(raw) else True  # (smaller id, larger id)
+    got = oracle.canonical(raw)
+    assert len(got) == len(raw), "duplicate pairs"
+    return got
+
+
+# ---- box construction -----------------------------------------------------------
+
+def test_build_kat_meshes(ctx, stq, kat, cuda):
+    for name, m in kat["meshes"].items():
+        arrays = decode_mesh(m)
+        out, n = build_dev(ctx, arrays, cuda, m["r"])
+        got = to_host_boxes(out, n, stq)
+        want = decode_boxes(m["boxes"], stq.AABB_DTYPE)
+        assert got.tobytes() == want.tobytes(), name
+
+
+def test_build_cloth_fixture(ctx, stq, cloth_fixture, cuda):
+    f = cloth_fixture
+    out, n = build_dev(ctx, (f["V0"], f["V1"], f["E"], f["F"]), cuda)
+    got = to_host_boxes(out, n, stq)
+    assert np.array_equal(got["min"].view(np.uint32), f["box_min"].view(np.uint32))
+    assert np.array_equal(got["max"].view(np.uint32), f["box_max"].view(np.uint32))
+    assert np.array_equal(got["vertex_ids"], f["vertex_ids"])
+
+
+@pytest.mark.parametrize("r", [0.0, 1e-4, 2.5e-3])
+def test_build_cloth_pair_vs_oracle(ctx, stq, oracle, cuda, r):
+    m = stq.cloth_pair(g=200, seed=0)
+    out, n = build_dev(ctx, (m.V0, m.V1, m.E, m.F), cuda, r)
+    got = to_host_boxes(out, n, stq)
+    want = oracle.construct_boxes(m.V0, m.V1, m.E, m.F, stq.AABB_DTYPE, r)
+    assert got.tobytes() == want.tobytes()
+
+
+def test_build_rejects_bad_index(ctx, stq, cuda):
+    m = stq.cloth_pair(g=8, seed=1)
+    E = m.E.copy()
+    E[3, 1] = m.V0.shape[0]
+    with pytest.raises(stq.STQError) as e:
+        build_dev(ctx, (m.V0, m.V1, E, m.F), cuda)
+    assert e.value.status == stq.STQ_ERR_INVALID_INPUT
+
+
+# ---- sweep ------------------------------------------------------------------------
+
+@pytest.mark.parametrize("axis", [-1, 0, 1, 2])
+def test_sweep_kat_cases(ctx, stq, oracle, kat, cuda, axis):
+    for name, case in kat["pairs"].items():
+        boxes = decode_boxes(case["boxes"], stq.AABB_DTYPE)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, expected_pairs(case["expected"])), (name, axis)
+
+
+def test_sweep_kat_meshes_device_built(ctx, stq, oracle, kat, cuda):
+    for name, m in kat["meshes"].items():
+        out, n = build_dev(ctx, decode_mesh(m), cuda, m["r"])
+        got = sweep_pairs(ctx, stq, oracle, out, n, cuda, -1)
+        assert np.array_equal(got, expected_pairs(m["expected"])), name
+
+
+def test_sweep_cloth_fixture(ctx, stq, oracle, cloth_fixture, cuda):
+    f = cloth_fixture
+    out, n = build_dev(ctx, (f["V0"], f["V1"], f["E"], f["F"]), cuda)
+    for axis in (-1, 0, 1, 2):
+        assert np.array_equal(sweep_pairs(ctx, stq, oracle, out, n, cuda, axis), f["pairs"])
+
+
+@pytest.fixture(scope="module")
+def c0(stq, oracle):
+    """The single-scene cloth pair: 2 sheets of 200^2 vertices, 476,806 boxes."""
+    m = stq.cloth_pair(g=200, seed=0)
+    boxes = oracle.construct_boxes(m.V0, m.V1, m.E, m.F, stq.AABB_DTYPE)
+    return m, boxes, oracle.broadphase(boxes)
+
+
+@pytest.mark.parametrize("axis", [-1, 0, 1, 2])
+def test_sweep_cloth_pair_vs_oracle(ctx, stq, oracle, cuda, c0, axis):
+    m, boxes, want = c0
+    out, n = build_dev(ctx, (m.V0, m.V1, m.E, m.F), cuda)
+    got = sweep_pairs(ctx, stq, oracle, out, n, cuda, axis)
+    assert np.array_equal(got, want)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
+@pytest.mark.parametrize("queue", [32, 64, 128])
+@pytest.mark.parametrize("block", [128, 256, 512])
+def test_sweep_tuning_space(ctx, stq, oracle, cuda, c0, lanes, queue, block):
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_LANES, lanes)
+    ctx.set_option(stq.OPT_QUEUE, queue)
+    ctx.set_option(stq.OPT_BLOCK, block)
+    got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
+    assert np.array_equal(got, want)
+
+
+def test_sweep_radix_4bit(ctx, stq, oracle, cuda, c0):
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_RADIX_BITS, 4)
+    assert np.array_equal(sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 1), want)
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_sweep_skewed_boxes_vs_oracle(ctx, stq, oracle, cuda, seed):
+    boxes = stq.random_boxes(200_000, sliver_frac=0.05, seed=seed)
+    want = oracle.broadphase(boxes)
+    for axis in (0, -1):
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, want), axis
+
+
+def test_sweep_ids_are_box_ids_not_positions(ctx, stq, oracle, cuda, c0):
+    m, boxes, want = c0
+    rng = np.random.default_rng(0)
+    perm = rng.permutation(len(boxes))
+    shuffled = boxes[perm]
+    got = sweep_pairs(ctx, stq, oracle, boxes_dev(shuffled, cuda), len(boxes), cuda, 0)
+    assert np.array_equal(got, want)
+
+
+# ---- overflow and resume ---------------------------------------------------------------
+
+@pytest.mark.parametrize("div", [2, 7, 50])
+def test_overflow_resume_covers_everything_once(ctx, stq, oracle, cuda, c0, div):
+    import torch
+
+    m, boxes, want = c0
+    cap = len(want) // div + 1
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    ctx.prepare(boxes_dev(boxes, cuda), len(boxes), 0)
+    start, chunks, calls = 0, [], 0
+    while start < len(boxes):
+        r = ctx.sweep_prepared(pairs, cap, start=start)
+        assert r.count <= cap
+        assert r.next_start > start
+        if r.next_start < len(boxes):
+            assert r.status == stq.STQ_OVERFLOW
+        chunks.append(pairs[: r.count].cpu().numpy().copy())
+        start = r.next_start
+        calls += 1
+    assert calls >= div
+    allp = np.concatenate(chunks)
+    got = oracle.canonical(allp)
+    assert len(got) == len(allp)
+    assert np.array_equal(got, want)
+
+
+def test_max_start_batches(ctx, stq, oracle, cuda, c0):
+    """The reference's MAX_OVERLAP_CUTOFF batching over start boxes with the
+    tidstart cursor (src/simulation.cu:239, 747)."""
+    import torch
+
+    m, boxes, want = c0
+    cap = len(want)
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
+    start, parts = 0, []
+    while start < len(boxes):
+        r = ctx.sweep_prepared(pairs, cap, start=start, max_start=len(boxes) // 5 + 1)
+        assert r.status == stq.STQ_OK
+        parts.append(pairs[: r.count].cpu().numpy().copy())
+        start = r.next_start
+    assert len(parts) == 5
+    assert np.array_equal(oracle.canonical(np.concatenate(parts)), want)
+
+
+def test_capacity_too_small_for_one_box(ctx, stq, cuda):
+    import torch
+
+    boxes = np.zeros(6, stq.AABB_DTYPE)
+    for i in range(6):
+        boxes[i] = (i, [0, 0, 0], [1, 1, 1], [i, -i - 1, -i - 1] if i == 0 else [10 + i, 20 + i, 30 + i], i)
+    pairs = torch.empty((2, 2), dtype=torch.int32, device=cuda)
+    with pytest.raises(stq.STQError) as e:
+        ctx.sweep(boxes_dev(boxes, cuda), 6, pairs, 2)
+    assert e.value.status == stq.STQ_ERR_CAPACITY
+
+
+# ---- edge cases ---------------------------------------------------------------------------
+
+def test_empty_and_tiny(ctx, stq, oracle, cuda):
+    import torch
+
+    pairs = torch.empty((4, 2), dtype=torch.int32, device=cuda)
+    r = ctx.sweep(None, 0, pairs, 4)
+    assert (r.status, r.count, r.next_start) == (stq.STQ_OK, 0, 0)
+    one = np.zeros(1, stq.AABB_DTYPE)
+    one[0] = (0, [0, 0, 0], [1, 1, 1], [0, -1, -1], 0)
+    r = ctx.sweep(boxes_dev(one, cuda), 1, pairs, 4)
+    assert (r.status, r.count, r.next_start) == (stq.STQ_OK, 0, 1)
+    r = ctx.sweep(boxes_dev(one, cuda), 1, pairs, 0)
+    assert r.count == 0
+
+
+def test_nan_bound_rejected(ctx, stq, cuda):
+    import torch
+
+    boxes = stq.random_boxes(1000, seed=5)
+    boxes[417]["max"][2] = np.nan
+    pairs = torch.empty((100000, 2), dtype=torch.int32, device=cuda)
+    with pytest.raises(stq.STQError) as e:
+        ctx.sweep(boxes_dev(boxes, cuda), len(boxes), pairs, 100000)
+    assert e.value.status == stq.STQ_ERR_INVALID_INPUT
+
+
+def test_invalid_arguments(ctx, stq, cuda):
+    import torch
+
+    pairs = torch.empty((4, 2), dtype=torch.int32, device=cuda)
+    with pytest.raises(stq.STQError):
+        ctx.sweep(None, -1, pairs, 4)
+    with pytest.raises(stq.STQError):
+        ctx.set_option(stq.OPT_LANES, 3)
+    ctx2 = stq.Context(0)
+    with pytest.raises(stq.STQError) as e:
+        ctx2.sweep_prepared(pairs, 4)
+    assert e.value.status == stq.STQ_ERR_NOT_PREPARED
+    ctx2.close()
+
+
+# ---- other entry points ---------------------------------------------------------------------
+
+def test_brute_force_agrees(ctx, stq, oracle, cuda):
+    import torch
+
+    boxes = stq.random_boxes(4000, seed=8)
+    c = 0.5 * (boxes["min"] + boxes["max"])
+    boxes["min"], boxes["max"] = c - 0.03, c + 0.03
+    want = oracle.broadphase(boxes)
+    cap = 4 * len(want) + 16
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    n = ctx.brute_force(boxes_dev(boxes, cuda), len(boxes), pairs, cap)
+    assert np.array_equal(oracle.canonical(pairs[:n].cpu().numpy()), want)
+    assert np.array_equal(sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1), want)
+
+
+def test_sort_pairs_lexicographic(ctx, stq, oracle, cuda, c0):
+    import torch
+
+    m, boxes, want = c0
+    cap = len(want)
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    r = ctx.sweep(boxes_dev(boxes, cuda), len(boxes), pairs, cap)
+    ctx.sort_pairs(pairs, r.count)
+    assert np.array_equal(pairs[: r.count].cpu().numpy(), want)
+
+
+def test_sweep_host_end_to_end(stq, oracle, cuda, c0):
+    m, boxes, want = c0
+    with stq.Context(0) as ctx:
+        out = np.empty((len(want) + 10, 2), np.int32)
+        r = ctx.sweep_host(boxes, out)
+        assert r.status == stq.STQ_OK and r.count == len(want)
+        assert np.array_equal(oracle.canonical(out[: r.count]), want)
+        small = np.empty((len(want) // 3, 2), np.int32)
+        r = ctx.sweep_host(boxes, small)
+        assert r.status == stq.STQ_OVERFLOW and r.total == len(want) and r.count <= len(small)
+        assert ctx.launches > 0
+
+
+def test_prepared_scene_reused_across_windows(ctx, stq, oracle, cuda, c0):
+    import torch
+
+    m, boxes, want = c0
+    pairs = torch.empty((len(want), 2), dtype=torch.int32, device=cuda)
+    bd = boxes_dev(boxes, cuda)
+    ctx.prepare(bd, len(boxes), 2)
+    del bd  # the prepared scene does not keep the input buffer
+    torch.cuda.empty_cache()
+    r1 = ctx.sweep_prepared(pairs, len(want), start=0, max_start=100_000)
+    a = pairs[: r1.count].cpu().numpy().copy()
+    r2 = ctx.sweep_prepared(pairs, len(want), start=r1.next_start)
+    b = pairs[: r2.count].cpu().numpy().copy()
+    assert np.array_equal(oracle.canonical(np.concatenate([a, b])), want)
