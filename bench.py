@@ -1,0 +1,344 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 STQ broad phase: boxes/s and pairs/s.
+
+Default workload: the large single scene, 16 interpenetrating crumpled sheets
+of 250 x 250 vertices (5,968,048 vertex/edge/face boxes), synthetic and
+seeded (the reference's external mesh benchmarks are not distributed).
+
+One step = device box build from fp64 trajectories -> sweep-axis choice ->
+radix sort -> STQ sweep -> all pairs in HBM. `value` times the step with its
+inputs resident in HBM (CUDA events on the library's stream, L2 flushed
+between steps); `e2e` times the same step through the C ABI on host buffers
+(stq_broadphase_host: H2D mesh copy, pipeline, D2H pair copy).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl stq|reference]
+
+--impl reference times the reference's CPU sweep restated in oracle/ (the
+reference library itself cannot be built here) on the host cores.
+Under torchrun (N > 1) every rank runs an independent replica (the path does
+not shard on one scene); rank 0 prints the JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOADS = {
+    "crumpled16x250": dict(kind="crumpled", sheets=16, g=250, amp=0.05, sigma=0.005, seed=1),
+    "crumpled16x290": dict(kind="crumpled", sheets=16, g=290, amp=0.05, sigma=0.005, seed=1),
+    "cloth200": dict(kind="cloth", g=200, z_offset=0.01, sigma=0.003, seed=0),
+}
+L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2
+FALLBACK_HBM_GBS = 6800.0
+
+
+def make_mesh(stq, w):
+    if w["kind"] == "crumpled":
+        return stq.crumpled_sheets(w["sheets"], w["g"], w["amp"], w["sigma"], w["seed"])
+    return stq.cloth_pair(g=w["g"], z_offset=w["z_offset"], sigma=w["sigma"], seed=w["seed"])
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / "traffic.txt"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        parts = line.split()
+        if len(parts) >= 3 and parts[0] == kernel and parts[1] == workload:
+            try:
+                return int(parts[2])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) >= 9:
+                try:
+                    rows.append((float(f[1]), float(f[2]), f[5:9]))
+                except ValueError:
+                    pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def cpu_baseline(stq, orc, boxes, budget_s: float, threads: int = 0):
+    """Oracle sort of all boxes + sweep of every stride-th start box, scaled to
+    the full scene: boxes/s of the reference's CPU algorithm on this host."""
+    n = len(boxes)
+    t_sort, t_sweep, _ = orc.time_sample(boxes, 1024, threads)
+    est_full = t_sweep * 1024
+    stride = 1
+    while est_full / stride > budget_s * 0.5 and stride < (1 << 20):
+        stride *= 2
+    if stride != 1024:
+        t_sort, t_sweep, _ = orc.time_sample(boxes, stride, threads)
+    t_full = t_sort + t_sweep * stride
+    th = threads if threads > 0 else orc.default_threads()
+    return dict(value=n / t_full, unit="boxes/s", cores=th, kind="port",
+                sample=(f"oracle sort of all {n} boxes ({t_sort:.2f} s) + sweep of every {stride}-th "
+                        f"start box ({t_sweep:.2f} s), scaled x{stride}"),
+                t_sort_s=t_sort, t_sweep_sample_s=t_sweep, stride=stride, t_full_s=t_full)
+
+
+def run_reference(args, w):
+    import __graft_entry__ as entry
+
+    pkg = entry.load_package()
+    stq = pkg.stq
+    orc = entry.load_oracle()
+    orc.build()
+    mesh = make_mesh(stq, w)
+    boxes = orc.construct_boxes(mesh.V0, mesh.V1, mesh.E, mesh.F, stq.AABB_DTYPE)
+    n = len(boxes)
+    probe = cpu_baseline(stq, orc, boxes, budget_s=args.ref_step_s)
+    stride = probe["stride"]
+    times = []
+    for i in range(args.warmup + args.steps):
+        t_sort, t_sweep, _ = orc.time_sample(boxes, stride, 0)
+        if i >= args.warmup:
+            times.append(t_sort + t_sweep * stride)
+    t = sum(times) / len(times)
+    value = n / t
+    line = {
+        "metric": "boxes/s (STQ broad phase, one scene)", "value": value, "unit": "boxes/s",
+        "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic",
+        "config": {"workload": args.workload, "boxes": n, "host_threads": probe["cores"]},
+        "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": probe["cores"], "kind": "port",
+                         "sample": probe["sample"]},
+        "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="stq", choices=["stq", "reference"])
+    ap.add_argument("--workload", default="crumpled16x250", choices=sorted(WORKLOADS))
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--ref-step-s", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    w = WORKLOADS[args.workload]
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if rank == 0:
+            run_reference(args, w)
+        return
+
+    import numpy as np
+    import torch
+
+    import __graft_entry__ as entry
+
+    pkg = entry.load_package()
+    stq = pkg.stq
+    torch.cuda.set_device(local)
+    dev = torch.device(f"cuda:{local}")
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=dev)
+
+    mesh = make_mesh(stq, w)
+    nV, nE, nF = mesh.V0.shape[0], mesh.E.shape[0], mesh.F.shape[0]
+    n = nV + nE + nF
+    stream = torch.cuda.Stream(dev)
+    V0 = torch.from_numpy(mesh.V0).to(dev)
+    V1 = torch.from_numpy(mesh.V1).to(dev)
+    E = torch.from_numpy(mesh.E).to(dev)
+    F = torch.from_numpy(mesh.F).to(dev)
+    boxes = torch.empty((n, 11), dtype=torch.int32, device=dev)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
+    torch.cuda.synchronize(dev)
+
+    ctx = stq.Context(local, stream.cuda_stream)
+    # size the pair buffer from a first run
+    cap = 1 << 20
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    ctx.build_boxes(V0, V1, E, F, boxes)
+    ctx.prepare(boxes, n, stq.AXIS_AUTO)
+    r = ctx.sweep_prepared(pairs, cap)
+    cap = int(r.total * 1.05) + 1024
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+
+    def step():
+        ctx.build_boxes(V0, V1, E, F, boxes)
+        ctx.prepare(boxes, n, stq.AXIS_AUTO)
+        res = ctx.sweep_prepared(pairs, cap)
+        assert res.status == stq.STQ_OK, res
+        return res.count
+
+    for _ in range(args.warmup):
+        flush.fill_(1)
+        step()
+    torch.cuda.synchronize(dev)
+    ctx.enable_timing(True)
+    launches0 = ctx.launches
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        for i in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i)  # evict the previous step's working set from L2
+            evs[i][0].record(stream)
+            npairs = step()
+            evs[i][1].record(stream)
+        torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    launches = ctx.launches - launches0
+    stages = ctx.stage_times()
+    ctx.enable_timing(False)
+    ms_per_step = total_ms / args.steps
+    value = world * n / (ms_per_step / 1e3)
+
+    # dominant kernel and its roofline (algorithmic bytes per launch / launch time)
+    dom = max(stages.items(), key=lambda kv: kv[1][0])
+    dom_name, (dom_ms, dom_calls) = dom
+    alg_bytes = {
+        "sweep": 40 * n + 8 * npairs,             # sorted records read once, pairs written once
+        "sort": 16 * n,                           # key+index read once and written once
+        "build": 24 * 2 * nV + 8 * nE + 12 * nF + 44 * n,
+        "gather": 44 * n + 40 * n,
+    }.get(dom_name)
+    peak, peak_kind = measured_peak()
+    per_launch_ms = dom_ms / max(dom_calls, 1)
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if alg_bytes else None
+    traffic = ncu_traffic(dom_name, args.workload)
+
+    line = {
+        "metric": "boxes/s (STQ broad phase, one scene)", "value": value, "unit": "boxes/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded crumpled-sheet trajectories; the reference's mesh benchmarks are not distributed)",
+        "config": {"workload": args.workload, "boxes": n, "vertices": nV, "edges": nE, "faces": nF,
+                   "pairs": npairs, "axis": "max-variance", "l2": "flushed between steps (512 MB write)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "pairs_per_s": world * npairs / (ms_per_step / 1e3),
+        "stage_ms_per_step": {k: v[0] / args.steps for k, v in stages.items() if v[1]},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic, "peak_source": f"{peak_kind} hbm_gbs",
+                     "alg_bytes_per_launch": alg_bytes, "launch_ms": per_launch_ms},
+        "pipeline_alg_frac": (60 * n + 8 * npairs) / (ms_per_step / 1e3) / 1e9 / peak,
+        "clocks": clk.summary(),
+    }
+
+    if not args.no_e2e:
+        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
+        hmesh = stq.Mesh(pin(mesh.V0), pin(mesh.V1), pin(mesh.E), pin(mesh.F))
+        hpairs = torch.empty((cap, 2), dtype=torch.int32).pin_memory().numpy()
+        ectx = stq.Context(local, stream.cuda_stream)
+        for _ in range(args.warmup):
+            ectx.broadphase_host(hmesh, hpairs, stq.AXIS_AUTO)
+        ts = []
+        for _ in range(args.steps):
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            er = ectx.broadphase_host(hmesh, hpairs, stq.AXIS_AUTO)
+            ts.append(time.perf_counter() - t0)
+        assert er.status == stq.STQ_OK and er.count == npairs, er
+        e2e_s = sum(ts) / len(ts)
+        if dist:
+            t = torch.tensor([e2e_s], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        line["e2e"] = {"value": world * n / e2e_s, "unit": "boxes/s",
+                       "h2d_bytes_per_step": 48 * nV + 8 * nE + 12 * nF,
+                       "d2h_bytes_per_step": 8 * er.count, "ms_per_step": e2e_s * 1e3,
+                       "call": "stq_broadphase_host"}
+        ectx.close()
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        orc = entry.load_oracle()
+        hb = orc.construct_boxes(mesh.V0, mesh.V1, mesh.E, mesh.F, stq.AABB_DTYPE)
+        cb = cpu_baseline(stq, orc, hb, budget_s=args.cpu_budget_s)
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    ctx.close()
+    if dist:
+        dist.destroy_process_group()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

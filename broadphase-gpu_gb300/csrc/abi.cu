@@ -19,6 +19,11 @@
 
 using namespace stq;
 
+constexpr int kStages = 8;
+const char *const kStageNames[kStages] = {"build", "axis", "keys", "sort",
+                                          "gather", "sweep", "count_sweep", "pair_sort"};
+enum Stage { kBuild, kAxis, kKeys, kSort, kGather, kSweep, kCountSweep, kPairSort };
+
 struct stq_context {
   int device = 0;
   int num_sms = 152;
@@ -38,8 +43,14 @@ struct stq_context {
   DevBuf keys[2], vals[2], sort_ws, scalars, partials, box_counts, prefix_ws;
   DevBuf pair_keys[2];
   // end-to-end staging
-  DevBuf e2e_boxes, e2e_pairs;
+  DevBuf e2e_boxes, e2e_pairs, e2e_mesh;
   DevScalars *h_scalars = nullptr;  // pinned readback
+  // stage timers
+  bool timing = false;
+  cudaEvent_t ev[kStages][2] = {};
+  bool pending[kStages] = {};
+  double stage_ms[kStages] = {};
+  int64_t stage_calls[kStages] = {};
 };
 
 namespace {
@@ -90,6 +101,33 @@ __global__ void reset_sweep_kernel(DevScalars *s) {
   s->work = 0;
 }
 
+void collect_stage(stq_context *ctx, int st) {
+  if (!ctx->pending[st]) return;
+  float ms = 0.f;
+  if (cudaEventSynchronize(ctx->ev[st][1]) == cudaSuccess &&
+      cudaEventElapsedTime(&ms, ctx->ev[st][0], ctx->ev[st][1]) == cudaSuccess) {
+    ctx->stage_ms[st] += ms;
+    ctx->stage_calls[st] += 1;
+  }
+  ctx->pending[st] = false;
+}
+
+void collect_stages(stq_context *ctx) {
+  for (int st = 0; st < kStages; ++st) collect_stage(ctx, st);
+}
+
+void stage_begin(stq_context *ctx, int st) {
+  if (!ctx->timing) return;
+  collect_stage(ctx, st);
+  cudaEventRecord(ctx->ev[st][0], ctx->stream);
+}
+
+void stage_end(stq_context *ctx, int st) {
+  if (!ctx->timing) return;
+  cudaEventRecord(ctx->ev[st][1], ctx->stream);
+  ctx->pending[st] = true;
+}
+
 void apply_options(stq_context *ctx) {
   SweepTuning t;
   if (ctx->options[STQ_OPT_LANES_PER_ENTRY]) t.lanes = int(ctx->options[STQ_OPT_LANES_PER_ENTRY]);
@@ -104,6 +142,7 @@ int read_scalars(stq_context *ctx) {
                                 cudaMemcpyDeviceToHost, ctx->stream),
            "read back sweep counters");
   STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  collect_stages(ctx);
   if (ctx->h_scalars->flags & kFlagNaN)
     return fail(ctx, STQ_ERR_INVALID_INPUT, "a box bound is NaN");
   if (ctx->h_scalars->flags & kFlagBadIndex)
@@ -130,8 +169,10 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.box_counts = ctx->box_counts.as<int32_t>();
   reset_sweep_kernel<<<1, 1, 0, ctx->stream>>>(ds);
   STQ_CUDA(ctx, cudaGetLastError(), "reset sweep counters");
+  stage_begin(ctx, count_mode ? kCountSweep : kSweep);
   STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms),
            "launch sweep");
+  stage_end(ctx, count_mode ? kCountSweep : kSweep);
   ctx->launches += (end > begin) ? 2 : 1;
   return STQ_OK;
 }
@@ -190,7 +231,11 @@ void stq_context_destroy(stq_context *ctx) {
                       &ctx->partials, &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0],
                       &ctx->pair_keys[1], &ctx->e2e_boxes, &ctx->e2e_pairs})
       b->release();
+    ctx->e2e_mesh.release();
     if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+    for (int st = 0; st < kStages; ++st)
+      for (int k = 0; k < 2; ++k)
+        if (ctx->ev[st][k]) cudaEventDestroy(ctx->ev[st][k]);
   }
   delete ctx;
 }
@@ -244,25 +289,42 @@ const char *stq_context_last_error(const stq_context *ctx) {
 
 int64_t stq_context_launch_count(const stq_context *ctx) { return ctx ? ctx->launches : -1; }
 
-int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
-                    const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
-                    float inflation_radius, stq_aabb *d_boxes) {
-  if (!ctx) return STQ_ERR_INVALID_ARG;
+}  // extern "C"
+
+namespace {
+
+int enqueue_build(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
+                  const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
+                  float inflation_radius, stq_aabb *d_boxes) {
   if (nV < 0 || nE < 0 || nF < 0 || nV + nE + nF > kMaxBoxes)
     return fail(ctx, STQ_ERR_INVALID_ARG, "box counts out of range");
   if ((nV > 0 && (!d_V0 || !d_V1)) || (nE > 0 && !d_E) || (nF > 0 && !d_F) ||
       (nV + nE + nF > 0 && !d_boxes))
     return fail(ctx, STQ_ERR_INVALID_ARG, "null buffer");
-  if (nV + nE + nF == 0) return STQ_OK;
-  DeviceGuard g(ctx->device);
   const float r_up = ref_next_up(inflation_radius);
   DevScalars *ds = ctx->scalars.as<DevScalars>();
   init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, 0);
   STQ_CUDA(ctx, cudaGetLastError(), "init counters");
+  stage_begin(ctx, kBuild);
   STQ_CUDA(ctx, launch_build_boxes(ctx->stream, d_V0, d_V1, nV, d_E, nE, d_F, nF, r_up,
                                    d_boxes, &ds->flags),
            "launch box build");
-  ctx->launches += 2;
+  stage_end(ctx, kBuild);
+  ctx->launches += (nV + nE + nF > 0) ? 2 : 1;
+  return STQ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
+                    const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
+                    float inflation_radius, stq_aabb *d_boxes) {
+  if (!ctx) return STQ_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  const int st = enqueue_build(ctx, d_V0, d_V1, nV, d_E, nE, d_F, nF, inflation_radius, d_boxes);
+  if (st != STQ_OK) return st;
   return read_scalars(ctx);
 }
 
@@ -308,26 +370,34 @@ int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis) 
   if (axis == STQ_AXIS_AUTO && n > 0) {
     const int nb = axis_partial_blocks(n);
     STQ_CUDA(ctx, ctx->partials.ensure(sizeof(double) * 6 * nb), "allocate axis partials");
+    stage_begin(ctx, kAxis);
     STQ_CUDA(ctx, launch_axis_select(ctx->stream, d_boxes, n, ctx->partials.as<double>(), nb,
                                      &ds->axis),
              "launch axis selection");
+    stage_end(ctx, kAxis);
     ctx->launches += 2;
   }
   uint32_t *kb[2] = {ctx->keys[0].as<uint32_t>(), ctx->keys[1].as<uint32_t>()};
   uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
+  stage_begin(ctx, kKeys);
   STQ_CUDA(ctx, launch_prep_keys(ctx->stream, d_boxes, n, &ds->axis, kb[0], vb[0], &ds->flags),
            "launch key preparation");
+  stage_end(ctx, kKeys);
   ctx->launches += n > 0 ? 1 : 0;
   int which = 0;
+  stage_begin(ctx, kSort);
   STQ_CUDA(ctx, radix_sort_u32(ctx->stream, kb, vb, n, ctx->radix_bits, ctx->sort_ws.ptr, &which,
                                &ctx->launches),
            "launch radix sort");
+  stage_end(ctx, kSort);
   ctx->scene.sx = ctx->sx.as<float2>();
   ctx->scene.syz = ctx->syz.as<float4>();
   ctx->scene.sv = ctx->sv.as<int4>();
   ctx->scene.length = n;
+  stage_begin(ctx, kGather);
   STQ_CUDA(ctx, launch_gather(ctx->stream, d_boxes, vb[which], n, &ds->axis, ctx->scene),
            "launch gather");
+  stage_end(ctx, kGather);
   ctx->launches += 1;
   ctx->n = n;
   ctx->prepared = true;
@@ -432,15 +502,94 @@ int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count) {
   STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(count, 8, 8)), "allocate sort workspace");
   unsigned long long *kb[2] = {ctx->pair_keys[0].as<unsigned long long>(),
                                ctx->pair_keys[1].as<unsigned long long>()};
+  stage_begin(ctx, kPairSort);
   STQ_CUDA(ctx, launch_pairs_to_keys(ctx->stream, d_pairs, count, kb[0], true), "pairs to keys");
   int which = 0;
   STQ_CUDA(ctx, radix_sort_u64(ctx->stream, kb, count, 0, 64, ctx->sort_ws.ptr, &which,
                                &ctx->launches),
            "launch pair sort");
   STQ_CUDA(ctx, launch_pairs_to_keys(ctx->stream, d_pairs, count, kb[which], false), "keys to pairs");
+  stage_end(ctx, kPairSort);
   ctx->launches += 2;
   STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  collect_stages(ctx);
   return STQ_OK;
+}
+
+int stq_broadphase_host(stq_context *ctx, const double *h_V0, const double *h_V1, int64_t nV,
+                        const int32_t *h_E, int64_t nE, const int32_t *h_F, int64_t nF,
+                        float inflation_radius, int axis, stq_pair *h_pairs, int64_t capacity,
+                        int64_t *count, int64_t *total) {
+  if (!ctx) return STQ_ERR_INVALID_ARG;
+  if (nV < 0 || nE < 0 || nF < 0 || nV + nE + nF > kMaxBoxes || capacity < 0 || !count ||
+      (capacity > 0 && !h_pairs) || (nV > 0 && (!h_V0 || !h_V1)) || (nE > 0 && !h_E) ||
+      (nF > 0 && !h_F))
+    return fail(ctx, STQ_ERR_INVALID_ARG, "invalid host mesh arguments");
+  DeviceGuard g(ctx->device);
+  auto up16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+  const size_t bv = sizeof(double) * 3 * size_t(nV), be = sizeof(int32_t) * 2 * size_t(nE),
+               bf = sizeof(int32_t) * 3 * size_t(nF);
+  const size_t oV1 = up16(bv), oE = oV1 + up16(bv), oF = oE + up16(be);
+  STQ_CUDA(ctx, ctx->e2e_mesh.ensure(oF + up16(bf) + 16), "allocate mesh staging");
+  const int64_t n = nV + nE + nF;
+  STQ_CUDA(ctx, ctx->e2e_boxes.ensure(sizeof(stq_aabb) * size_t(n > 0 ? n : 1)),
+           "allocate box staging");
+  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1)),
+           "allocate pair staging");
+  char *base = ctx->e2e_mesh.as<char>();
+  if (bv) {
+    STQ_CUDA(ctx, cudaMemcpyAsync(base, h_V0, bv, cudaMemcpyHostToDevice, ctx->stream), "copy V0");
+    STQ_CUDA(ctx, cudaMemcpyAsync(base + oV1, h_V1, bv, cudaMemcpyHostToDevice, ctx->stream), "copy V1");
+  }
+  if (be) STQ_CUDA(ctx, cudaMemcpyAsync(base + oE, h_E, be, cudaMemcpyHostToDevice, ctx->stream), "copy E");
+  if (bf) STQ_CUDA(ctx, cudaMemcpyAsync(base + oF, h_F, bf, cudaMemcpyHostToDevice, ctx->stream), "copy F");
+  int st = enqueue_build(ctx, reinterpret_cast<const double *>(base),
+                         reinterpret_cast<const double *>(base + oV1), nV,
+                         reinterpret_cast<const int32_t *>(base + oE), nE,
+                         reinterpret_cast<const int32_t *>(base + oF), nF, inflation_radius,
+                         ctx->e2e_boxes.as<stq_aabb>());
+  if (st != STQ_OK) return st;
+  st = stq_prepare(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis);
+  if (st != STQ_OK) return st;
+  int64_t next = 0;
+  st = stq_sweep_prepared(ctx, 0, 0, ctx->e2e_pairs.as<stq_pair>(), capacity, count, &next, total);
+  if (st != STQ_OK && st != STQ_OVERFLOW) return st;
+  if (*count > 0) {
+    STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, ctx->e2e_pairs.ptr, sizeof(stq_pair) * size_t(*count),
+                                  cudaMemcpyDeviceToHost, ctx->stream),
+             "copy pairs to host");
+    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  }
+  return st;
+}
+
+int stq_context_enable_timing(stq_context *ctx, int enable) {
+  if (!ctx) return STQ_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  if (enable && !ctx->ev[0][0]) {
+    for (int st = 0; st < kStages; ++st)
+      for (int k = 0; k < 2; ++k)
+        STQ_CUDA(ctx, cudaEventCreate(&ctx->ev[st][k]), "create timing event");
+  }
+  if (!enable) collect_stages(ctx);
+  ctx->timing = enable != 0;
+  for (int st = 0; st < kStages; ++st) ctx->stage_ms[st] = 0.0, ctx->stage_calls[st] = 0;
+  return STQ_OK;
+}
+
+int stq_context_stage_times(stq_context *ctx, double *ms, int64_t *calls, int max_stages) {
+  if (!ctx || max_stages < 0) return STQ_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  collect_stages(ctx);
+  for (int st = 0; st < kStages && st < max_stages; ++st) {
+    if (ms) ms[st] = ctx->stage_ms[st];
+    if (calls) calls[st] = ctx->stage_calls[st];
+  }
+  return kStages;
+}
+
+const char *stq_stage_name(int stage) {
+  return (stage >= 0 && stage < kStages) ? kStageNames[stage] : "unknown";
 }
 
 int stq_brute_force(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, stq_pair *d_pairs,

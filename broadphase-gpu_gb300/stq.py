@@ -67,6 +67,13 @@ ABI_SIGNATURES = {
                                  ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p, _c_i64p, _c_i64p]),
     "stq_sweep_host": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, _vp, ctypes.c_int64,
                                       _c_i64p, _c_i64p]),
+    "stq_broadphase_host": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp,
+                                           ctypes.c_int64, ctypes.c_float, ctypes.c_int, _vp,
+                                           ctypes.c_int64, _c_i64p, _c_i64p]),
+    "stq_context_enable_timing": (ctypes.c_int, [_vp, ctypes.c_int]),
+    "stq_context_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _c_i64p,
+                                               ctypes.c_int]),
+    "stq_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
     "stq_sort_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "stq_brute_force": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p]),
 }
@@ -214,6 +221,30 @@ class Context:
                                      ctypes.byref(tot))
         self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
         return SweepResult(st, c.value, boxes.shape[0], tot.value)
+
+    def broadphase_host(self, mesh: "Mesh", pairs: np.ndarray, axis: int = AXIS_AUTO,
+                        inflation_radius: float = 0.0) -> SweepResult:
+        """Host mesh in (ideally pinned), host pairs (int32 [cap, 2]) out: copies,
+        device box build, sort and sweep in one native call."""
+        for a in (mesh.V0, mesh.V1, mesh.E, mesh.F, pairs):
+            assert a.flags.c_contiguous
+        c, tot = ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_broadphase_host(
+            self._h, mesh.V0.ctypes.data, mesh.V1.ctypes.data, mesh.V0.shape[0],
+            mesh.E.ctypes.data, mesh.E.shape[0], mesh.F.ctypes.data, mesh.F.shape[0],
+            float(inflation_radius), axis, pairs.ctypes.data, pairs.shape[0], ctypes.byref(c),
+            ctypes.byref(tot))
+        self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
+        return SweepResult(st, c.value, mesh.num_boxes, tot.value)
+
+    def enable_timing(self, enable: bool = True) -> None:
+        self._check(self.lib.stq_context_enable_timing(self._h, int(enable)))
+
+    def stage_times(self) -> dict:
+        ms = (ctypes.c_double * 16)()
+        calls = (ctypes.c_int64 * 16)()
+        k = self.lib.stq_context_stage_times(self._h, ms, calls, 16)
+        return {self.lib.stq_stage_name(i).decode(): (ms[i], calls[i]) for i in range(k)}
 
     def sort_pairs(self, pairs, count: int) -> None:
         self._check(self.lib.stq_sort_pairs(self._h, _ptr(pairs), count))

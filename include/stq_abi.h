@@ -23,6 +23,9 @@
  *   stq_sweep_host       <- the same call with host boxes in and host pairs
  *                           out (H2D at simulation.cu:580, KEEP_CPU_OVERLAPS
  *                           copy-back at simulation.cu:763-780)
+ *   stq_broadphase_host  <- constructBoxes + run_sweep_sharedqueue on host
+ *                           meshes (app/main.cu:82-144)
+ *   stq_context_*timing* <- CudaTimer / recordLaunch   src/timer.cuh:7-72
  *   stq_brute_force      <- get_collision_pairs (all-pairs checker)
  *                           src/collision.cu:91-154
  */
@@ -143,6 +146,27 @@ int stq_sweep(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis,
 int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n,
                    int axis, stq_pair *h_pairs, int64_t capacity,
                    int64_t *count, int64_t *total);
+
+/* End-to-end call on a host mesh: copies V0/V1 ([nV x 3] fp64), E and F
+ * (int32) to the device, builds the swept boxes, sweeps every start box and
+ * copies the pairs back to h_pairs (capacity entries). The reference path
+ * this replaces is constructBoxes on the host followed by
+ * run_sweep_sharedqueue with KEEP_CPU_OVERLAPS (app/main.cu:83-144). */
+int stq_broadphase_host(stq_context *ctx, const double *h_V0, const double *h_V1,
+                        int64_t nV, const int32_t *h_E, int64_t nE,
+                        const int32_t *h_F, int64_t nF, float inflation_radius,
+                        int axis, stq_pair *h_pairs, int64_t capacity,
+                        int64_t *count, int64_t *total);
+
+/* Per-stage device timers (CUDA events on the context's stream; replaces
+ * the reference's CudaTimer / recordLaunch, src/timer.cuh:7-72). Stages:
+ * 0 build, 1 axis, 2 keys, 3 sort, 4 gather, 5 sweep, 6 count sweep,
+ * 7 pair sort. stq_context_stage_times fills up to max_stages entries of
+ * accumulated milliseconds and call counts and returns the stage count. */
+int stq_context_enable_timing(stq_context *ctx, int enable);
+int stq_context_stage_times(stq_context *ctx, double *ms, int64_t *calls,
+                            int max_stages);
+const char *stq_stage_name(int stage);
 
 /* Sorts d_pairs[0..count) lexicographically on the device (deterministic
  * output order for callers that need one). */
