@@ -24,6 +24,13 @@ const char *const kStageNames[kStages] = {"build", "axis", "keys", "sort",
                                           "gather", "sweep", "count_sweep", "pair_sort"};
 enum Stage { kBuild, kAxis, kKeys, kSort, kGather, kSweep, kCountSweep, kPairSort };
 
+// Grid and replica count of the prepared scene, read back once per prepare.
+struct PrepInfo {
+  GridParams grid;
+  uint32_t replicas;
+  uint32_t pad;
+};
+
 struct stq_context {
   int device = 0;
   int num_sms = 152;
@@ -42,6 +49,10 @@ struct stq_context {
   // sort and sweep scratch
   DevBuf keys[2], vals[2], sort_ws, scalars, partials, box_counts, prefix_ws;
   DevBuf pair_keys[2];
+  // cells mode
+  DevBuf stats, prep, counts, offsets, scan_ws, keys64[2], scell;
+  PrepInfo *h_prep = nullptr;  // pinned readback
+  float cell_scale = 4.f;
   // end-to-end staging
   DevBuf e2e_boxes, e2e_pairs, e2e_mesh;
   DevScalars *h_scalars = nullptr;  // pinned readback
@@ -135,6 +146,7 @@ void apply_options(stq_context *ctx) {
   if (ctx->options[STQ_OPT_BLOCK_SIZE]) t.block = int(ctx->options[STQ_OPT_BLOCK_SIZE]);
   ctx->tuning = t;
   ctx->radix_bits = ctx->options[STQ_OPT_RADIX_BITS] ? int(ctx->options[STQ_OPT_RADIX_BITS]) : 8;
+  ctx->cell_scale = ctx->options[STQ_OPT_CELL_SCALE] ? float(ctx->options[STQ_OPT_CELL_SCALE]) : 4.f;
 }
 
 int read_scalars(stq_context *ctx) {
@@ -167,6 +179,8 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.count = &ds->count;
   p.work = &ds->work;
   p.box_counts = ctx->box_counts.as<int32_t>();
+  p.scell = ctx->scene.scell;
+  p.grid = ctx->scene.scell ? &ctx->prep.as<PrepInfo>()->grid : nullptr;
   reset_sweep_kernel<<<1, 1, 0, ctx->stream>>>(ds);
   STQ_CUDA(ctx, cudaGetLastError(), "reset sweep counters");
   stage_begin(ctx, count_mode ? kCountSweep : kSweep);
@@ -211,7 +225,10 @@ int stq_context_create(int device, void *stream, stq_context **out) {
   DeviceGuard g(device);
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
   if (cudaMallocHost(&ctx->h_scalars, sizeof(DevScalars)) != cudaSuccess ||
-      ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess) {
+      cudaMallocHost(&ctx->h_prep, sizeof(PrepInfo)) != cudaSuccess ||
+      ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess ||
+      ctx->stats.ensure(sizeof(SceneStats)) != cudaSuccess ||
+      ctx->prep.ensure(sizeof(PrepInfo)) != cudaSuccess) {
     stq_context_destroy(ctx);
     return STQ_ERR_NO_MEMORY;
   }
@@ -232,7 +249,11 @@ void stq_context_destroy(stq_context *ctx) {
                       &ctx->pair_keys[1], &ctx->e2e_boxes, &ctx->e2e_pairs})
       b->release();
     ctx->e2e_mesh.release();
+    for (DevBuf *b : {&ctx->stats, &ctx->prep, &ctx->counts, &ctx->offsets, &ctx->scan_ws,
+                      &ctx->keys64[0], &ctx->keys64[1], &ctx->scell})
+      b->release();
     if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
+    if (ctx->h_prep) cudaFreeHost(ctx->h_prep);
     for (int st = 0; st < kStages; ++st)
       for (int k = 0; k < 2; ++k)
         if (ctx->ev[st][k]) cudaEventDestroy(ctx->ev[st][k]);
@@ -247,7 +268,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 5 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 6 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -264,6 +285,12 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
     case STQ_OPT_RADIX_BITS:
       if (value != 0 && value != 4 && value != 8) return fail(ctx, STQ_ERR_INVALID_ARG, "radix bits: 4 or 8");
       break;
+    case STQ_OPT_CELLS:
+      if (value > 2048) return fail(ctx, STQ_ERR_INVALID_ARG, "cells: 0 (auto), 1 (off) or a grid side <= 2048");
+      break;
+    case STQ_OPT_CELL_SCALE:
+      if (value > 64) return fail(ctx, STQ_ERR_INVALID_ARG, "cell scale: 1..64");
+      break;
     default:
       break;
   }
@@ -273,12 +300,13 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 5) return -1;
+  if (!ctx || option < 1 || option > 6) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
     case STQ_OPT_BLOCK_SIZE: return ctx->tuning.block;
     case STQ_OPT_RADIX_BITS: return ctx->radix_bits;
+    case STQ_OPT_CELL_SCALE: return int64_t(ctx->cell_scale);
     default: return ctx->options[option];
   }
 }
@@ -352,56 +380,136 @@ int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis) 
   if (axis < STQ_AXIS_AUTO || axis > STQ_AXIS_Z) return fail(ctx, STQ_ERR_INVALID_ARG, "axis");
   DeviceGuard g(ctx->device);
   ctx->prepared = false;
-  const size_t slots = size_t(n) + 1 + kSortedPad;
-  STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
-  STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
-  STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
-  const size_t nn = size_t(n > 0 ? n : 1);
-  for (int b = 0; b < 2; ++b) {
-    STQ_CUDA(ctx, ctx->keys[b].ensure(sizeof(uint32_t) * nn), "allocate sort keys");
-    STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * nn), "allocate sort values");
-  }
-  STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(n, 4, ctx->radix_bits)),
-           "allocate sort workspace");
   DevScalars *ds = ctx->scalars.as<DevScalars>();
+  PrepInfo *pi = ctx->prep.as<PrepInfo>();
   init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, axis < 0 ? 0 : axis);
   STQ_CUDA(ctx, cudaGetLastError(), "init counters");
   ctx->launches += 1;
-  if (axis == STQ_AXIS_AUTO && n > 0) {
-    const int nb = axis_partial_blocks(n);
-    STQ_CUDA(ctx, ctx->partials.ensure(sizeof(double) * 6 * nb), "allocate axis partials");
-    stage_begin(ctx, kAxis);
-    STQ_CUDA(ctx, launch_axis_select(ctx->stream, d_boxes, n, ctx->partials.as<double>(), nb,
-                                     &ds->axis),
-             "launch axis selection");
-    stage_end(ctx, kAxis);
-    ctx->launches += 2;
+  // 1. statistics, sweep axis and cell grid (device), read back once
+  STQ_CUDA(ctx, ctx->partials.ensure(stats_partials_bytes(n)), "allocate statistics");
+  stage_begin(ctx, kAxis);
+  STQ_CUDA(ctx, launch_scene_stats(ctx->stream, d_boxes, n, ctx->partials.as<double>(),
+                                   ctx->stats.as<SceneStats>(), &ds->flags),
+           "launch scene statistics");
+  STQ_CUDA(ctx, launch_grid_policy(ctx->stream, ctx->partials.as<double>(), n,
+                                   ctx->stats.as<SceneStats>(), axis,
+                                   int(ctx->options[STQ_OPT_CELLS]), ctx->cell_scale, &pi->grid,
+                                   &ds->axis),
+           "launch grid policy");
+  stage_end(ctx, kAxis);
+  ctx->launches += 3;
+  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_prep, pi, sizeof(PrepInfo), cudaMemcpyDeviceToHost,
+                                ctx->stream),
+           "read back grid");
+  int st = read_scalars(ctx);
+  if (st != STQ_OK) return st;
+  const GridParams grid = ctx->h_prep->grid;
+  const size_t nn = size_t(n > 0 ? n : 1);
+
+  if (grid.ncells <= 1) {
+    // 2a. one cell: 32-bit keys, the sort of the reference's create_ds path
+    const size_t slots = size_t(n) + 1 + kSortedPad;
+    STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
+    STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
+    STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
+    for (int b = 0; b < 2; ++b) {
+      STQ_CUDA(ctx, ctx->keys[b].ensure(sizeof(uint32_t) * nn), "allocate sort keys");
+      STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * nn), "allocate sort values");
+    }
+    STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(n, 4, ctx->radix_bits)),
+             "allocate sort workspace");
+    uint32_t *kb[2] = {ctx->keys[0].as<uint32_t>(), ctx->keys[1].as<uint32_t>()};
+    uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
+    stage_begin(ctx, kKeys);
+    STQ_CUDA(ctx, launch_prep_keys(ctx->stream, d_boxes, n, &ds->axis, kb[0], vb[0], &ds->flags),
+             "launch key preparation");
+    stage_end(ctx, kKeys);
+    ctx->launches += n > 0 ? 1 : 0;
+    int which = 0;
+    stage_begin(ctx, kSort);
+    STQ_CUDA(ctx, radix_sort_u32(ctx->stream, kb, vb, n, ctx->radix_bits, ctx->sort_ws.ptr,
+                                 &which, &ctx->launches),
+             "launch radix sort");
+    stage_end(ctx, kSort);
+    ctx->scene.sx = ctx->sx.as<float2>();
+    ctx->scene.syz = ctx->syz.as<float4>();
+    ctx->scene.sv = ctx->sv.as<int4>();
+    ctx->scene.scell = nullptr;
+    ctx->scene.length = n;
+    stage_begin(ctx, kGather);
+    STQ_CUDA(ctx, launch_gather(ctx->stream, d_boxes, vb[which], n, &ds->axis, ctx->scene),
+             "launch gather");
+    stage_end(ctx, kGather);
+    ctx->launches += 1;
+    ctx->n = n;
+    ctx->prepared = true;
+    return STQ_OK;
   }
-  uint32_t *kb[2] = {ctx->keys[0].as<uint32_t>(), ctx->keys[1].as<uint32_t>()};
-  uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
+
+  // 2b. cells: replicate each box into the cells it touches
+  STQ_CUDA(ctx, ctx->counts.ensure(sizeof(uint32_t) * nn), "allocate replica counts");
+  STQ_CUDA(ctx, ctx->offsets.ensure(sizeof(uint32_t) * nn), "allocate replica offsets");
+  STQ_CUDA(ctx, ctx->scan_ws.ensure(scan_workspace_bytes(n)), "allocate scan workspace");
   stage_begin(ctx, kKeys);
-  STQ_CUDA(ctx, launch_prep_keys(ctx->stream, d_boxes, n, &ds->axis, kb[0], vb[0], &ds->flags),
-           "launch key preparation");
+  STQ_CUDA(ctx, launch_replica_count(ctx->stream, d_boxes, n, &pi->grid,
+                                     ctx->counts.as<uint32_t>()),
+           "launch replica count");
+  STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, ctx->counts.as<uint32_t>(),
+                                   ctx->offsets.as<uint32_t>(), n, ctx->scan_ws.ptr,
+                                   &pi->replicas, &ctx->launches),
+           "launch replica scan");
+  ctx->launches += 1;
+  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_prep, pi, sizeof(PrepInfo), cudaMemcpyDeviceToHost,
+                                ctx->stream),
+           "read back replica count");
+  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  const int64_t R = ctx->h_prep->replicas;
+  if (R < n || R + grid.ncells + 1 + kSortedPad > int64_t(INT32_MAX))
+    return fail(ctx, STQ_ERR_NO_MEMORY, "too many cell replicas for 32-bit positions");
+  const size_t slots = size_t(R) + size_t(grid.ncells) + 1 + kSortedPad;
+  STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->scell.ensure(sizeof(int) * slots), "allocate sorted scene");
+  for (int b = 0; b < 2; ++b) {
+    STQ_CUDA(ctx, ctx->keys64[b].ensure(sizeof(unsigned long long) * size_t(R)), "allocate keys");
+    STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * size_t(R)), "allocate values");
+  }
+  STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(R, 8, 8)), "allocate sort workspace");
+  unsigned long long *kb[2] = {ctx->keys64[0].as<unsigned long long>(),
+                               ctx->keys64[1].as<unsigned long long>()};
+  uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
+  STQ_CUDA(ctx, launch_replica_emit(ctx->stream, d_boxes, n, &pi->grid,
+                                    ctx->offsets.as<uint32_t>(), kb[0], vb[0]),
+           "launch replica emit");
   stage_end(ctx, kKeys);
-  ctx->launches += n > 0 ? 1 : 0;
+  ctx->launches += 1;
   int which = 0;
   stage_begin(ctx, kSort);
-  STQ_CUDA(ctx, radix_sort_u32(ctx->stream, kb, vb, n, ctx->radix_bits, ctx->sort_ws.ptr, &which,
-                               &ctx->launches),
+  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, R, 0, 32 + grid.cell_bits,
+                                    ctx->sort_ws.ptr, &which, &ctx->launches),
            "launch radix sort");
   stage_end(ctx, kSort);
   ctx->scene.sx = ctx->sx.as<float2>();
   ctx->scene.syz = ctx->syz.as<float4>();
   ctx->scene.sv = ctx->sv.as<int4>();
-  ctx->scene.length = n;
+  ctx->scene.scell = ctx->scell.as<int>();
+  ctx->scene.length = R + grid.ncells;
   stage_begin(ctx, kGather);
-  STQ_CUDA(ctx, launch_gather(ctx->stream, d_boxes, vb[which], n, &ds->axis, ctx->scene),
+  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, int64_t(slots)),
+           "launch sentinel fill");
+  STQ_CUDA(ctx, launch_gather_cells(ctx->stream, d_boxes, kb[which], vb[which], R, &pi->grid,
+                                    ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
-  ctx->launches += 1;
+  ctx->launches += 2;
   ctx->n = n;
   ctx->prepared = true;
   return STQ_OK;
+}
+
+int64_t stq_prepared_length(const stq_context *ctx) {
+  return (ctx && ctx->prepared) ? ctx->scene.length : -1;
 }
 
 int stq_sweep_prepared(stq_context *ctx, int64_t start, int64_t max_start, stq_pair *d_pairs,

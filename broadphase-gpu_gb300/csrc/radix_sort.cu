@@ -253,4 +253,81 @@ cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2], int64_t 
                                                  workspace, which, launches);
 }
 
+cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2], uint32_t *vbuf[2],
+                                int64_t n, int begin_bit, int end_bit, void *workspace,
+                                int *which, int64_t *launches) {
+  return sort_impl<unsigned long long, 8, true>(s, kbuf, vbuf, n, begin_bit, end_bit,
+                                                workspace, which, launches);
+}
+
+// ---- exclusive scan of uint32 counts (reduce-then-scan, no waiting) -------------
+namespace {
+
+constexpr int kScanItems = 8;
+constexpr int kScanTile = kSortBlock * kScanItems;
+
+__global__ void __launch_bounds__(kSortBlock)
+scan_reduce_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ sums) {
+  __shared__ uint32_t scratch[32];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+  uint32_t s = 0;
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) s += in[base + i];
+  uint32_t tot;
+  block_exclusive_scan(s, &tot, scratch);
+  if (threadIdx.x == 0) sums[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(kSortBlock)
+scan_sums_kernel(uint32_t *__restrict__ sums, int64_t ntiles, uint32_t *__restrict__ total) {
+  __shared__ uint32_t scratch[32];
+  uint32_t carry = 0;
+  for (int64_t b = 0; b < ntiles; b += kSortBlock) {
+    const int64_t i = b + threadIdx.x;
+    const uint32_t v = i < ntiles ? sums[i] : 0;
+    uint32_t tot;
+    const uint32_t ex = block_exclusive_scan(v, &tot, scratch);
+    if (i < ntiles) sums[i] = carry + ex;
+    carry += tot;
+  }
+  if (threadIdx.x == 0) *total = carry;
+}
+
+__global__ void __launch_bounds__(kSortBlock)
+scan_apply_kernel(const uint32_t *__restrict__ in, int64_t n, const uint32_t *__restrict__ sums,
+                  uint32_t *__restrict__ out) {
+  __shared__ uint32_t scratch[32];
+  const int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t s = 0;
+  for (int i = 0; i < kScanItems; ++i) {
+    v[i] = base + i < n ? in[base + i] : 0;
+    s += v[i];
+  }
+  uint32_t tot;
+  uint32_t run = sums[blockIdx.x] + block_exclusive_scan(s, &tot, scratch);
+  for (int i = 0; i < kScanItems; ++i) {
+    if (base + i < n) out[base + i] = run;
+    run += v[i];
+  }
+}
+
+}  // namespace
+
+size_t scan_workspace_bytes(int64_t n) {
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  return sizeof(uint32_t) * size_t(ntiles + 1);
+}
+
+cudaError_t exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n,
+                               void *workspace, uint32_t *d_total, int64_t *launches) {
+  const int64_t ntiles = (n + kScanTile - 1) / kScanTile;
+  uint32_t *sums = static_cast<uint32_t *>(workspace);
+  if (n > 0) scan_reduce_kernel<<<unsigned(ntiles), kSortBlock, 0, s>>>(in, n, sums);
+  scan_sums_kernel<<<1, kSortBlock, 0, s>>>(sums, ntiles, d_total);
+  if (n > 0) scan_apply_kernel<<<unsigned(ntiles), kSortBlock, 0, s>>>(in, n, sums, out);
+  if (launches) *launches += n > 0 ? 3 : 1;
+  return cudaGetLastError();
+}
+
 }  // namespace stq

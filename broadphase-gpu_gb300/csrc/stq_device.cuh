@@ -64,6 +64,16 @@ __device__ __forceinline__ uint32_t float_key(float f) {
   return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
 
+// Cell coordinate of a bound: clamp(floor((v - origin) * inv), 0, n - 1),
+// with round-to-nearest float steps. Each step is monotone non-decreasing in
+// v, so a <= b implies cell(a) <= cell(b): a point inside a box's range has
+// its cell inside the box's cell range.
+__device__ __forceinline__ int cell_coord(float v, float origin, float inv, int n) {
+  float t = __fmul_rn(__fsub_rn(v, origin), inv);
+  t = fminf(fmaxf(t, 0.f), float(n - 1));
+  return int(t);
+}
+
 // ---- box type and pair filter ------------------------------------------------
 // Type from the signs of vertexIds (src/aabb.cu:12-31): vertex {v,-v-1,-v-1}
 // -> 0, edge {e0,e1,-e0-1} -> 1, face {f0,f1,f2} -> 2.

@@ -50,6 +50,30 @@ enum : int {
   kFlagBadIndex = 2,   // an edge or face index is outside [0, nV)
 };
 
+// Cell grid on the two non-sweep axes b, c (the other two axes in increasing
+// order). A box is replicated into every cell its [min, max] range touches;
+// cell coordinates are a monotone function of the bound, so a pair that
+// overlaps shares the cell of its reference point (max of mins on b and c)
+// and is emitted there only.
+struct GridParams {
+  int axis;       // sweep axis a
+  int nb, nc;     // cells along b and c
+  int ncells;     // nb * nc
+  int cell_bits;  // bits of the largest cell id
+  int inverted;   // some box has min > max on b or c: cells disabled
+  float ob, oc;   // grid origin on b and c
+  float ib, ic;   // cells per unit length on b and c
+};
+
+// Per-scene statistics gathered in one pass over the boxes.
+struct SceneStats {
+  unsigned int lo_key[3];   // order-preserving min of the minima
+  unsigned int hi_key[3];   // order-preserving max of the maxima
+  unsigned int hist[3][64]; // log2 histogram of the box extents
+  int inverted;             // some box has min > max
+  int pad;
+};
+
 // Sweep-kernel tuning (autotuned or set through stq_context_set_option).
 struct SweepTuning {
   int lanes = 8;        // lanes sharing one pending start box (1..32)
@@ -64,6 +88,7 @@ struct SortedScene {
   float2 *sx = nullptr;   // (min, max) on the sweep axis
   float4 *syz = nullptr;  // (min_b, min_c, max_b, max_c) on the other axes
   int4 *sv = nullptr;     // (vertexIds[0..2], id)
+  int *scell = nullptr;   // cell id of each position (cells mode)
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
 
@@ -78,6 +103,8 @@ struct SweepParams {
   unsigned long long *count;
   int *work;
   int32_t *box_counts;       // count mode: pairs per start position (k - begin)
+  const int *scell;          // cells mode: cell id per position, else null
+  const GridParams *grid;    // cells mode: grid on the device
 };
 
 // ---- launch wrappers (each returns the launch error) -------------------------
@@ -97,6 +124,26 @@ cudaError_t launch_gather(cudaStream_t s, const stq_aabb *boxes,
                           const uint32_t *order, int64_t n, const int *d_axis,
                           SortedScene scene);
 
+// ---- cells mode ------------------------------------------------------------------
+// stats: one pass; grid: policy kernel (mode: -1 auto axis, else the axis;
+// cells_opt: 0 automatic, 1 no cells, k > 1 a k x k grid; scale: cell side
+// in median box extents)
+size_t stats_partials_bytes(int64_t n);
+cudaError_t launch_scene_stats(cudaStream_t s, const stq_aabb *boxes, int64_t n,
+                               double *partials, SceneStats *stats, int *flags);
+cudaError_t launch_grid_policy(cudaStream_t s, const double *partials, int64_t n,
+                               const SceneStats *stats, int axis_mode, int cells_opt,
+                               float scale, GridParams *grid, int *d_axis);
+cudaError_t launch_replica_count(cudaStream_t s, const stq_aabb *boxes, int64_t n,
+                                 const GridParams *grid, uint32_t *counts);
+cudaError_t launch_replica_emit(cudaStream_t s, const stq_aabb *boxes, int64_t n,
+                                const GridParams *grid, const uint32_t *offsets,
+                                unsigned long long *keys, uint32_t *vals);
+cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, int64_t slots);
+cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
+                                const unsigned long long *keys, const uint32_t *order,
+                                int64_t R, const GridParams *grid, SortedScene scene);
+
 // LSD radix sort of (uint32 key, uint32 value) or (uint64 key) pairs.
 // kbuf/vbuf are double buffers; *which receives the buffer index holding the
 // result. Returns workspace bytes when called with workspace == nullptr.
@@ -107,6 +154,13 @@ cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
 cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2],
                            int64_t n, int begin_bit, int end_bit, void *workspace,
                            int *which, int64_t *launches);
+cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2],
+                                uint32_t *vbuf[2], int64_t n, int begin_bit, int end_bit,
+                                void *workspace, int *which, int64_t *launches);
+// exclusive scan of n uint32 counts; *d_total receives the sum
+size_t scan_workspace_bytes(int64_t n);
+cudaError_t exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n,
+                               void *workspace, uint32_t *d_total, int64_t *launches);
 
 cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p,
                          const SweepTuning &t, bool count_mode, int num_sms);

@@ -21,7 +21,7 @@ namespace stq {
 
 namespace {
 
-template <int G, int Q, int BLOCK, bool COUNT>
+template <int G, int Q, int BLOCK, bool COUNT, bool CELLS>
 __global__ void __launch_bounds__(BLOCK)
 stq_sweep_kernel(const SweepParams p) {
   static_assert(32 % G == 0, "lane group must divide the warp");
@@ -47,6 +47,13 @@ stq_sweep_kernel(const SweepParams p) {
   float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
   int4 kv = make_int4(0, 0, 0, 0);
   const int span = p.end - p.begin;
+  // cells mode: grid and the cell of the current start box
+  float gob = 0.f, goc = 0.f, gib = 0.f, gic = 0.f;
+  int gnb = 1, gnc = 1, kcb = 0, kcc = 0;
+  if (CELLS) {
+    const GridParams g = *p.grid;
+    gob = g.ob, goc = g.oc, gib = g.ib, gic = g.ic, gnb = g.nb, gnc = g.nc;
+  }
 
   while (true) {
     // 1. Refill the ring with start boxes that have at least one candidate.
@@ -85,6 +92,11 @@ stq_sweep_kernel(const SweepParams p) {
         kb = p.syz[k];
         kv = p.sv[k];
         acc = 0;
+        if (CELLS) {
+          const int cell = p.scell[k];
+          kcb = cell / gnc;
+          kcc = cell - kcb * gnc;
+        }
       }
     }
     qhead = (qhead + ntake) & (Q - 1);
@@ -107,6 +119,11 @@ stq_sweep_kernel(const SweepParams p) {
       const float4 b = p.syz[j];
       const int4 bv = p.sv[j];
       hit = overlap_bc(kb, b) && valid_pair(kv, bv) && !covertex(kv, bv);
+      // a pair shared by several cells is emitted only in the cell of its
+      // reference point (max of the minima on b and c)
+      if (CELLS && hit)
+        hit = cell_coord(fmaxf(kb.x, b.x), gob, gib, gnb) == kcb &&
+              cell_coord(fmaxf(kb.y, b.y), goc, gic, gnc) == kcc;
       lo_id = min(kv.w, bv.w);
       hi_id = max(kv.w, bv.w);
     }
@@ -137,10 +154,10 @@ stq_sweep_kernel(const SweepParams p) {
   }
 }
 
-template <int G, int Q, int BLOCK>
-cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, bool count_mode, int num_sms) {
+template <int G, int Q, int BLOCK, bool COUNT, bool CELLS>
+cudaError_t launch_variant(cudaStream_t s, const SweepParams &p, int num_sms) {
   int per_sm = 0;
-  auto kern = count_mode ? stq_sweep_kernel<G, Q, BLOCK, true> : stq_sweep_kernel<G, Q, BLOCK, false>;
+  auto kern = stq_sweep_kernel<G, Q, BLOCK, COUNT, CELLS>;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
@@ -154,21 +171,27 @@ cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, bool count_mode, in
   return cudaGetLastError();
 }
 
+template <int G, int Q, int BLOCK>
+cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, int sms) {
+  return p.scell ? launch_variant<G, Q, BLOCK, false, true>(s, p, sms)
+                 : launch_variant<G, Q, BLOCK, false, false>(s, p, sms);
+}
+
 template <int G, int Q>
-cudaError_t launch_gq(cudaStream_t s, const SweepParams &p, int block, bool cm, int sms) {
+cudaError_t launch_gq(cudaStream_t s, const SweepParams &p, int block, int sms) {
   switch (block) {
-    case 128: return launch_gqb<G, Q, 128>(s, p, cm, sms);
-    case 512: return launch_gqb<G, Q, 512>(s, p, cm, sms);
-    default: return launch_gqb<G, Q, 256>(s, p, cm, sms);
+    case 128: return launch_gqb<G, Q, 128>(s, p, sms);
+    case 512: return launch_gqb<G, Q, 512>(s, p, sms);
+    default: return launch_gqb<G, Q, 256>(s, p, sms);
   }
 }
 
 template <int G>
-cudaError_t launch_g(cudaStream_t s, const SweepParams &p, const SweepTuning &t, bool cm, int sms) {
+cudaError_t launch_g(cudaStream_t s, const SweepParams &p, const SweepTuning &t, int sms) {
   switch (t.queue) {
-    case 32: return launch_gq<G, 32>(s, p, t.block, cm, sms);
-    case 128: return launch_gq<G, 128>(s, p, t.block, cm, sms);
-    default: return launch_gq<G, 64>(s, p, t.block, cm, sms);
+    case 32: return launch_gq<G, 32>(s, p, t.block, sms);
+    case 128: return launch_gq<G, 128>(s, p, t.block, sms);
+    default: return launch_gq<G, 64>(s, p, t.block, sms);
   }
 }
 
@@ -283,13 +306,16 @@ __global__ void pairs_keys_kernel(stq_pair *pairs, int64_t n, unsigned long long
 cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
                          bool count_mode, int num_sms) {
   if (p.end <= p.begin) return cudaSuccess;
+  if (count_mode)  // per-start-box counts do not depend on the tuning
+    return p.scell ? launch_variant<8, 64, 256, true, true>(s, p, num_sms)
+                   : launch_variant<8, 64, 256, true, false>(s, p, num_sms);
   switch (t.lanes) {
-    case 1: return launch_g<1>(s, p, t, count_mode, num_sms);
-    case 2: return launch_g<2>(s, p, t, count_mode, num_sms);
-    case 4: return launch_g<4>(s, p, t, count_mode, num_sms);
-    case 16: return launch_g<16>(s, p, t, count_mode, num_sms);
-    case 32: return launch_g<32>(s, p, t, count_mode, num_sms);
-    default: return launch_g<8>(s, p, t, count_mode, num_sms);
+    case 1: return launch_g<1>(s, p, t, num_sms);
+    case 2: return launch_g<2>(s, p, t, num_sms);
+    case 4: return launch_g<4>(s, p, t, num_sms);
+    case 16: return launch_g<16>(s, p, t, num_sms);
+    case 32: return launch_g<32>(s, p, t, num_sms);
+    default: return launch_g<8>(s, p, t, num_sms);
   }
 }
 

@@ -41,7 +41,7 @@ STQ_ERR_TIMEOUT = -6
 STQ_ERR_NOT_PREPARED = -7
 
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
-OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS = 1, 2, 3, 4, 5
+OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
@@ -61,6 +61,7 @@ ABI_SIGNATURES = {
                                        _vp, ctypes.c_int64, ctypes.c_float, _vp]),
     "stq_select_axis": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
     "stq_prepare": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int]),
+    "stq_prepared_length": (ctypes.c_int64, [_vp]),
     "stq_sweep_prepared": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int64, _vp, ctypes.c_int64,
                                           _c_i64p, _c_i64p, _c_i64p]),
     "stq_sweep": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.c_int, ctypes.c_int64,
@@ -195,6 +196,11 @@ class Context:
 
     def prepare(self, boxes, n: int, axis: int = AXIS_X) -> None:
         self._check(self.lib.stq_prepare(self._h, _ptr(boxes), n, axis))
+
+    @property
+    def prepared_length(self) -> int:
+        """Sweep positions of the prepared scene (the resume cursor's range)."""
+        return int(self.lib.stq_prepared_length(self._h))
 
     def sweep_prepared(self, pairs, capacity: int, start: int = 0, max_start: int = 0) -> SweepResult:
         c, nx, tot = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -85,8 +85,11 @@ typedef enum stq_option {
   STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1,2,4,8,16,32 */
   STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 32, 64 or 128           */
   STQ_OPT_BLOCK_SIZE = 3,      /* sweep block size: 128, 256 or 512               */
-  STQ_OPT_CELLS = 4,           /* y/z cell grid side (1 = no cells, 0 = automatic) */
-  STQ_OPT_RADIX_BITS = 5       /* radix digit width: 4 or 8                       */
+  STQ_OPT_CELLS = 4,           /* cell grid on the two non-sweep axes: 0 automatic,
+                                  1 no cells (plain sweep), k > 1 a k x k grid      */
+  STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
+  STQ_OPT_CELL_SCALE = 6       /* automatic cell side in median box extents (1..64,
+                                  default 4)                                        */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -123,6 +126,13 @@ int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
  * bounds, vertex ids). The boxes buffer may be reused after return. */
 int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
                 int axis);
+
+/* Number of sweep positions of the prepared scene: the start-box cursor of
+ * stq_sweep_prepared runs over [0, length). Equal to the box count when
+ * cells are off; with cells, boxes are replicated into the cells they touch
+ * and every cell is followed by one empty position. -1 if nothing is
+ * prepared. */
+int64_t stq_prepared_length(const stq_context *ctx);
 
 /* Sweeps start boxes [start, start + max_start) of the prepared scene in
  * sorted order (max_start <= 0 means all). Every overlapping pair whose

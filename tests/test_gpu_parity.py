@@ -43,7 +43,7 @@ def sweep_pairs(ctx, stq, oracle, bdev, n, cuda, axis=0, cap=None):
     pairs = torch.empty((max(cap, 1), 2), dtype=torch.int32, device=cuda)
     r = ctx.sweep(bdev, n, pairs, cap, axis=axis)
     assert r.status == stq.STQ_OK, r
-    assert r.count == r.total and r.next_start == n
+    assert r.count == r.total and r.next_start == ctx.prepared_length
     raw = pairs[: r.count].cpu().numpy()
     assert np.all(raw[:, 0] < raw[:, 1]) if len(raw) else True  # (smaller id, larger id)
     got = oracle.canonical(raw)
@@ -175,12 +175,13 @@ def test_overflow_resume_covers_everything_once(ctx, stq, oracle, cuda, c0, div)
     cap = len(want) // div + 1
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
     ctx.prepare(boxes_dev(boxes, cuda), len(boxes), 0)
+    length = ctx.prepared_length
     start, chunks, calls = 0, [], 0
-    while start < len(boxes):
+    while start < length:
         r = ctx.sweep_prepared(pairs, cap, start=start)
         assert r.count <= cap
         assert r.next_start > start
-        if r.next_start < len(boxes):
+        if r.next_start < length:
             assert r.status == stq.STQ_OVERFLOW
         chunks.append(pairs[: r.count].cpu().numpy().copy())
         start = r.next_start
@@ -200,15 +201,20 @@ def test_max_start_batches(ctx, stq, oracle, cuda, c0):
     m, boxes, want = c0
     cap = len(want)
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
-    ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
-    start, parts = 0, []
-    while start < len(boxes):
-        r = ctx.sweep_prepared(pairs, cap, start=start, max_start=len(boxes) // 5 + 1)
-        assert r.status == stq.STQ_OK
-        parts.append(pairs[: r.count].cpu().numpy().copy())
-        start = r.next_start
-    assert len(parts) == 5
-    assert np.array_equal(oracle.canonical(np.concatenate(parts)), want)
+    for cells in (1, 0):
+        ctx.set_option(stq.OPT_CELLS, cells)
+        ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
+        length = ctx.prepared_length
+        if cells == 1:
+            assert length == len(boxes)
+        start, parts = 0, []
+        while start < length:
+            r = ctx.sweep_prepared(pairs, cap, start=start, max_start=length // 5 + 1)
+            assert r.status == stq.STQ_OK
+            parts.append(pairs[: r.count].cpu().numpy().copy())
+            start = r.next_start
+        assert len(parts) == 5
+        assert np.array_equal(oracle.canonical(np.concatenate(parts)), want)
 
 
 def test_capacity_too_small_for_one_box(ctx, stq, cuda):
@@ -319,3 +325,71 @@ def test_prepared_scene_reused_across_windows(ctx, stq, oracle, cuda, c0):
     r2 = ctx.sweep_prepared(pairs, len(want), start=r1.next_start)
     b = pairs[: r2.count].cpu().numpy().copy()
     assert np.array_equal(oracle.canonical(np.concatenate([a, b])), want)
+
+
+# ---- cells (y/z grid segmentation with reference-point dedup) -------------------------
+
+@pytest.mark.parametrize("cells", [1, 2, 3, 7, 64, 512])
+def test_cells_fixed_grids(ctx, stq, oracle, cuda, c0, cells):
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_CELLS, cells)
+    for axis in (0, -1):
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, want), (cells, axis)
+        if cells == 1:
+            assert ctx.prepared_length == len(boxes)
+
+
+@pytest.mark.parametrize("scale", [1, 2, 4, 16])
+def test_cells_auto_scales(ctx, stq, oracle, cuda, c0, scale):
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_CELL_SCALE, scale)
+    for axis in (0, 1, 2):
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, want), (scale, axis)
+    assert ctx.prepared_length > len(boxes)  # replicas + one slot per cell
+
+
+def test_cells_skewed_slivers(ctx, stq, oracle, cuda):
+    boxes = stq.random_boxes(300_000, sliver_frac=0.05, seed=11)
+    want = oracle.broadphase(boxes)
+    for scale in (1, 4, 32):
+        ctx.set_option(stq.OPT_CELL_SCALE, scale)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1)
+        assert np.array_equal(got, want), scale
+
+
+def test_cells_inverted_and_infinite_boxes(ctx, stq, oracle, cuda):
+    boxes = stq.random_boxes(20_000, seed=12)
+    c = 0.5 * (boxes["min"] + boxes["max"])
+    boxes["min"], boxes["max"] = c - 0.01, c + 0.01
+    inv = boxes.copy()
+    inv["min"][::97, 1], inv["max"][::97, 1] = inv["max"][::97, 1], inv["min"][::97, 1]
+    inf = boxes.copy()
+    inf["max"][5, 2] = np.inf
+    inf["min"][9, 1] = -np.inf
+    for b in (inv, inf):
+        want = oracle.broadphase(b)
+        for cells in (0, 16):
+            ctx.set_option(stq.OPT_CELLS, cells)
+            got = sweep_pairs(ctx, stq, oracle, boxes_dev(b, cuda), len(b), cuda, -1)
+            assert np.array_equal(got, want)
+
+
+def test_cells_overflow_resume(ctx, stq, oracle, cuda):
+    import torch
+
+    boxes = stq.random_boxes(150_000, sliver_frac=0.05, seed=13)
+    want = oracle.broadphase(boxes)
+    cap = len(want) // 9 + 1
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    ctx.set_option(stq.OPT_CELLS, 32)
+    ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
+    start, chunks = 0, []
+    while start < ctx.prepared_length:
+        r = ctx.sweep_prepared(pairs, cap, start=start)
+        chunks.append(pairs[: r.count].cpu().numpy().copy())
+        start = r.next_start
+    allp = np.concatenate(chunks)
+    assert len(oracle.canonical(allp)) == len(allp)
+    assert np.array_equal(oracle.canonical(allp), want)
