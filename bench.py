@@ -222,7 +222,7 @@ def main():
 
     ctx = stq.Context(local, stream.cuda_stream)
     # size the pair buffer from a first run
-    cap = 1 << 20
+    cap = 24 * n
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     ctx.build_boxes(V0, V1, E, F, boxes)
     ctx.prepare(boxes, n, stq.AXIS_AUTO)

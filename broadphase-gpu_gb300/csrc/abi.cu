@@ -172,7 +172,11 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.sv = ctx->scene.sv;
   p.begin = int32_t(begin);
   p.end = int32_t(end);
-  p.chunk = ctx->tuning.chunk;
+  // start positions per work grab: at least ~4 grabs per resident warp
+  const int64_t span = end - begin;
+  const int64_t want = int64_t(ctx->num_sms) * 64 * 4;
+  int64_t chunk = ((span / want) + 31) / 32 * 32;
+  p.chunk = int32_t(chunk < 32 ? 32 : (chunk > ctx->tuning.chunk ? ctx->tuning.chunk : chunk));
   p.pairs = pairs;
   p.capacity = capacity;
   DevScalars *ds = ctx->scalars.as<DevScalars>();
