@@ -138,6 +138,59 @@ def cpu_baseline(stq, orc, boxes, budget_s: float, threads: int = 0):
                 t_sort_s=t_sort, t_sweep_sample_s=t_sweep, stride=stride, t_full_s=t_full)
 
 
+def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
+    """256 cloth-pair scenes (box counts log-uniform in [1e3, 2e5]): the fused,
+    graph-captured batch call against the per-scene plain launch loop
+    (build + prepare + sweep with its host synchronisations, scene by scene)."""
+    meshes = stq.batch_scenes(256, 1e3, 2e5, seed=2)
+    V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
+    d = [torch.from_numpy(x).to(dev) for x in (V0, V1, E, F)]
+    N = int(sum(m.num_boxes for m in meshes))
+    ctx = stq.Context(local, stream.cuda_stream)
+    cap = 64 * N
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    r, per = ctx.batch_broadphase(d[0], d[1], vo, d[2], eo, d[3], fo, pairs, cap)
+    total = r.total
+    cap = int(total * 1.05) + 1024
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        ms = 0.0
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms += a.elapsed_time(b)
+        return ms / steps
+
+    launches0 = ctx.launches
+    t_batch = timed(lambda: ctx.batch_broadphase(d[0], d[1], vo, d[2], eo, d[3], fo, pairs, cap))
+    boxes = torch.empty((max(m.num_boxes for m in meshes), 11), dtype=torch.int32, device=dev)
+
+    def plain_loop():
+        found = 0
+        for k, m in enumerate(meshes):
+            v = slice(int(vo[k]), int(vo[k + 1]))
+            ctx.build_boxes(d[0][v], d[1][v], d[2][int(eo[k]):int(eo[k + 1])],
+                            d[3][int(fo[k]):int(fo[k + 1])], boxes)
+            ctx.prepare(boxes, m.num_boxes, stq.AXIS_AUTO)
+            found += ctx.sweep_prepared(pairs, cap).count
+        assert found == total, (found, total)
+
+    t_plain = timed(plain_loop)
+    ctx.close()
+    return {"workload": "256 cloth-pair scenes, boxes log-uniform in [1e3, 2e5]", "boxes": N,
+            "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain,
+            "batched_boxes_per_s": N / (t_batch / 1e3), "plain_loop_boxes_per_s": N / (t_plain / 1e3),
+            "batched_over_plain": t_plain / t_batch, "graph": True}
+
+
 def run_reference(args, w):
     import __graft_entry__ as entry
 
@@ -181,6 +234,7 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -327,6 +381,9 @@ def main():
                        "d2h_bytes_per_step": 8 * er.count, "ms_per_step": e2e_s * 1e3,
                        "call": "stq_broadphase_host"}
         ectx.close()
+
+    if not args.no_batch:
+        line["batched"] = bench_batched(stq, torch, dev, stream, local, args.steps, args.warmup, flush)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = entry.load_oracle()

@@ -13,6 +13,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "stq_device.cuh"
 #include "stq_internal.h"
@@ -24,11 +25,40 @@ const char *const kStageNames[kStages] = {"build", "axis", "keys", "sort",
                                           "gather", "sweep", "count_sweep", "pair_sort"};
 enum Stage { kBuild, kAxis, kKeys, kSort, kGather, kSweep, kCountSweep, kPairSort };
 
-// Grid and replica count of the prepared scene, read back once per prepare.
-struct PrepInfo {
-  GridParams grid;
-  uint32_t replicas;
-  uint32_t pad;
+// Input block uploaded with one copy before every prepare: the batch header,
+// the scene offsets (boxes, and vertices/edges/faces for batched builds), the
+// per-scene options and the tile table. Offsets are fixed by the capacities.
+struct Staging {
+  int scene_cap = 0, tile_cap = 0;
+  size_t hdr = 0, box_off = 0, voff = 0, eoff = 0, foff = 0, inputs = 0, tiles = 0, total = 0;
+  static Staging make(int scene_cap, int tile_cap) {
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    Staging st;
+    st.scene_cap = scene_cap;
+    st.tile_cap = tile_cap;
+    size_t o = 0;
+    st.hdr = o, o = up(o + sizeof(BatchHeader));
+    const size_t offs = sizeof(long long) * size_t(scene_cap + 1);
+    st.box_off = o, o = up(o + offs);
+    st.voff = o, o = up(o + offs);
+    st.eoff = o, o = up(o + offs);
+    st.foff = o, o = up(o + offs);
+    st.inputs = o, o = up(o + sizeof(SceneInput) * size_t(scene_cap));
+    st.tiles = o, o = up(o + sizeof(TileRec) * size_t(tile_cap));
+    st.total = o;
+    return st;
+  }
+};
+
+struct GraphKey {
+  const void *ptr[6] = {};
+  int64_t sizes[8] = {};
+  int64_t opts[10] = {};
+  cudaStream_t stream = nullptr;
+  bool operator==(const GraphKey &o) const {
+    return std::memcmp(ptr, o.ptr, sizeof ptr) == 0 && std::memcmp(sizes, o.sizes, sizeof sizes) == 0 &&
+           std::memcmp(opts, o.opts, sizeof opts) == 0 && stream == o.stream;
+  }
 };
 
 struct stq_context {
@@ -38,24 +68,39 @@ struct stq_context {
   std::string error;
   int64_t launches = 0;
   SweepTuning tuning;
-  int64_t options[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  int radix_bits = 8;
+  int64_t options[16] = {};
+  float cell_scale = 2.f;
+  int budget = 4;
 
-  // sorted scene
+  // capacities of the batch buffers
+  int scene_cap = 0, tile_cap = 0;
+  int64_t box_cap = 0, rep_cap = 0, slot_cap = 0;
+  Staging layout;
+  DevBuf in_dev;
+  char *in_host = nullptr;
+  size_t in_host_bytes = 0;
+  DevBuf scenes, cell_base, scene_pairs, counts, offsets, scan_ws, keys64[2], vals[2], sort_ws;
+  DevBuf sx, syz, sv, sflag, box_counts, prefix_ws, pair_keys[2];
+  DevBuf batch_boxes, e2e_boxes, e2e_pairs, e2e_mesh;
+  DevBuf aux;  // header of calls outside a batch (box build, all-pairs check)
+
+  // prepared batch (host view)
   bool prepared = false;
-  int64_t n = 0;
+  int n_scenes = 0;
+  int64_t n_boxes = 0, length = 0;
   SortedScene scene;
-  DevBuf sx, syz, sv;
-  // sort and sweep scratch
-  DevBuf keys[2], vals[2], sort_ws, scalars, partials, box_counts, prefix_ws;
-  DevBuf pair_keys[2];
-  // cells mode
-  DevBuf stats, prep, counts, offsets, scan_ws, keys64[2], scell;
-  PrepInfo *h_prep = nullptr;  // pinned readback
-  float cell_scale = 4.f;
-  // end-to-end staging
-  DevBuf e2e_boxes, e2e_pairs, e2e_mesh;
-  DevScalars *h_scalars = nullptr;  // pinned readback
+  BatchHeader *h_hdr = nullptr;             // pinned readback
+  unsigned long long *h_scene_pairs = nullptr;  // pinned readback
+  int h_scene_pairs_cap = 0;
+
+  // captured graph of stq_batch_broadphase, on a private stream (the legacy
+  // default stream cannot be captured)
+  cudaStream_t graph_stream = nullptr;
+  cudaEvent_t graph_event = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  GraphKey graph_key;
+  bool capturing = false;
+
   // stage timers
   bool timing = false;
   cudaEvent_t ev[kStages][2] = {};
@@ -99,18 +144,11 @@ int fail(stq_context *ctx, int status, const char *what, cudaError_t e = cudaSuc
                   (what), _e);                                           \
   } while (0)
 
-__global__ void init_scalars_kernel(DevScalars *s, int axis) {
-  s->count = 0;
-  s->work = 0;
-  s->flags = 0;
-  s->prefix = 0;
-  s->axis = axis;
-}
-
-__global__ void reset_sweep_kernel(DevScalars *s) {
-  s->count = 0;
-  s->work = 0;
-}
+#define STQ_TRY(expr)              \
+  do {                             \
+    const int _st = (expr);        \
+    if (_st != STQ_OK) return _st; \
+  } while (0)
 
 void collect_stage(stq_context *ctx, int st) {
   if (!ctx->pending[st]) return;
@@ -128,13 +166,13 @@ void collect_stages(stq_context *ctx) {
 }
 
 void stage_begin(stq_context *ctx, int st) {
-  if (!ctx->timing) return;
+  if (!ctx->timing || ctx->capturing) return;
   collect_stage(ctx, st);
   cudaEventRecord(ctx->ev[st][0], ctx->stream);
 }
 
 void stage_end(stq_context *ctx, int st) {
-  if (!ctx->timing) return;
+  if (!ctx->timing || ctx->capturing) return;
   cudaEventRecord(ctx->ev[st][1], ctx->stream);
   ctx->pending[st] = true;
 }
@@ -145,53 +183,274 @@ void apply_options(stq_context *ctx) {
   if (ctx->options[STQ_OPT_QUEUE_DEPTH]) t.queue = int(ctx->options[STQ_OPT_QUEUE_DEPTH]);
   if (ctx->options[STQ_OPT_BLOCK_SIZE]) t.block = int(ctx->options[STQ_OPT_BLOCK_SIZE]);
   ctx->tuning = t;
-  ctx->radix_bits = ctx->options[STQ_OPT_RADIX_BITS] ? int(ctx->options[STQ_OPT_RADIX_BITS]) : 8;
-  ctx->cell_scale = ctx->options[STQ_OPT_CELL_SCALE] ? float(ctx->options[STQ_OPT_CELL_SCALE]) : 4.f;
+  ctx->cell_scale = ctx->options[STQ_OPT_CELL_SCALE] ? float(ctx->options[STQ_OPT_CELL_SCALE]) : 2.f;
+  ctx->budget = ctx->options[STQ_OPT_REPLICA_BUDGET] ? int(ctx->options[STQ_OPT_REPLICA_BUDGET]) : 4;
 }
 
-int read_scalars(stq_context *ctx) {
-  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_scalars, ctx->scalars.ptr, sizeof(DevScalars),
+BatchHeader *dev_hdr(stq_context *ctx) {
+  return reinterpret_cast<BatchHeader *>(ctx->in_dev.as<char>() + ctx->layout.hdr);
+}
+template <typename T>
+T *dev_at(stq_context *ctx, size_t off) {
+  return reinterpret_cast<T *>(ctx->in_dev.as<char>() + off);
+}
+template <typename T>
+T *host_at(stq_context *ctx, size_t off) {
+  return reinterpret_cast<T *>(ctx->in_host + off);
+}
+
+int read_header(stq_context *ctx, const BatchHeader *src = nullptr) {
+  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_hdr, src ? src : dev_hdr(ctx), sizeof(BatchHeader),
                                 cudaMemcpyDeviceToHost, ctx->stream),
-           "read back sweep counters");
+           "read back batch header");
   STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
   collect_stages(ctx);
-  if (ctx->h_scalars->flags & kFlagNaN)
-    return fail(ctx, STQ_ERR_INVALID_INPUT, "a box bound is NaN");
-  if (ctx->h_scalars->flags & kFlagBadIndex)
+  const int f = ctx->h_hdr->flags;
+  if (f & kFlagNaN) return fail(ctx, STQ_ERR_INVALID_INPUT, "a box bound is NaN");
+  if (f & kFlagBadIndex)
     return fail(ctx, STQ_ERR_INVALID_INPUT, "an edge or face vertex index is out of range");
+  if (f & kFlagReplicaOverflow)
+    return fail(ctx, STQ_ERR_NO_MEMORY, "cell replicas exceed the replica buffers");
   return STQ_OK;
 }
 
 constexpr int64_t kMaxBoxes = int64_t(INT32_MAX) - 4 * kSortedPad;
 
+int64_t tiles_for(const int64_t *box_off, int S) {
+  int64_t t = 0;
+  for (int s = 0; s < S; ++s) t += (box_off[s + 1] - box_off[s] + kTileBoxes - 1) / kTileBoxes;
+  return t;
+}
+
+// Grows the staging block (pinned host mirror and device copy).
+int ensure_staging(stq_context *ctx, int scene_cap, int tile_cap) {
+  if (scene_cap <= ctx->scene_cap && tile_cap <= ctx->tile_cap && ctx->in_host) return STQ_OK;
+  scene_cap = std::max(scene_cap, ctx->scene_cap);
+  tile_cap = std::max(tile_cap, ctx->tile_cap);
+  const Staging lay = Staging::make(scene_cap, tile_cap);
+  if (ctx->in_host) {
+    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+    cudaFreeHost(ctx->in_host);
+    ctx->in_host = nullptr;
+  }
+  STQ_CUDA(ctx, cudaMallocHost(&ctx->in_host, lay.total), "allocate pinned staging");
+  std::memset(ctx->in_host, 0, lay.total);
+  ctx->in_host_bytes = lay.total;
+  STQ_CUDA(ctx, ctx->in_dev.ensure(lay.total), "allocate staging");
+  STQ_CUDA(ctx, ctx->scenes.ensure(sizeof(SceneRecord) * size_t(scene_cap)), "allocate scenes");
+  STQ_CUDA(ctx, ctx->cell_base.ensure(sizeof(unsigned) * size_t(scene_cap + 1)), "allocate cell bases");
+  STQ_CUDA(ctx, ctx->scene_pairs.ensure(sizeof(unsigned long long) * size_t(scene_cap)),
+           "allocate scene pair counters");
+  if (scene_cap > ctx->h_scene_pairs_cap) {
+    if (ctx->h_scene_pairs) cudaFreeHost(ctx->h_scene_pairs);
+    ctx->h_scene_pairs = nullptr;
+    STQ_CUDA(ctx, cudaMallocHost(&ctx->h_scene_pairs, sizeof(unsigned long long) * size_t(scene_cap)),
+             "allocate pinned scene counters");
+    ctx->h_scene_pairs_cap = scene_cap;
+  }
+  ctx->layout = lay;
+  ctx->scene_cap = scene_cap;
+  ctx->tile_cap = tile_cap;
+  return STQ_OK;
+}
+
+// Writes the header, offsets, options and tiles into the pinned mirror.
+void fill_staging(stq_context *ctx, const int64_t *box_off, int S, const int *axes, int axis,
+                  const int64_t *voff, const int64_t *eoff, const int64_t *foff) {
+  const Staging &L = ctx->layout;
+  BatchHeader *h = host_at<BatchHeader>(ctx, L.hdr);
+  std::memset(h, 0, sizeof(BatchHeader));
+  h->n_boxes = box_off[S];
+  h->n_scenes = S;
+  h->budget = ctx->budget;
+  long long *bo = host_at<long long>(ctx, L.box_off);
+  for (int s = 0; s <= S; ++s) bo[s] = box_off[s];
+  if (voff) {
+    long long *v = host_at<long long>(ctx, L.voff), *e = host_at<long long>(ctx, L.eoff),
+              *f = host_at<long long>(ctx, L.foff);
+    for (int s = 0; s <= S; ++s) v[s] = voff[s], e[s] = eoff[s], f[s] = foff[s];
+  }
+  SceneInput *in = host_at<SceneInput>(ctx, L.inputs);
+  for (int s = 0; s < S; ++s) {
+    in[s].axis_mode = axes ? axes[s] : axis;
+    in[s].cells_opt = int(ctx->options[STQ_OPT_CELLS]);
+    in[s].cell_scale = ctx->cell_scale;
+    in[s].pad = 0;
+  }
+  TileRec *tr = host_at<TileRec>(ctx, L.tiles);
+  int t = 0;
+  for (int s = 0; s < S; ++s)
+    for (int64_t b = box_off[s]; b < box_off[s + 1]; b += kTileBoxes) {
+      tr[t].begin = b;
+      tr[t].count = int(std::min<int64_t>(kTileBoxes, box_off[s + 1] - b));
+      tr[t].scene = s;
+      ++t;
+    }
+  h->n_tiles = t;
+}
+
+int upload_staging(stq_context *ctx) {
+  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->in_dev.ptr, ctx->in_host, ctx->layout.total,
+                                cudaMemcpyHostToDevice, ctx->stream),
+           "upload batch inputs");
+  return STQ_OK;
+}
+
+BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
+  BatchBuffers b;
+  b.boxes = boxes;
+  b.box_off = dev_at<long long>(ctx, ctx->layout.box_off);
+  b.tiles = dev_at<TileRec>(ctx, ctx->layout.tiles);
+  b.tile_cap = ctx->tile_cap;
+  b.inputs = dev_at<SceneInput>(ctx, ctx->layout.inputs);
+  b.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
+  b.scenes = ctx->scenes.as<SceneRecord>();
+  b.cell_base = ctx->cell_base.as<unsigned>();
+  b.hdr = dev_hdr(ctx);
+  b.counts = ctx->counts.as<uint32_t>();
+  b.offsets = ctx->offsets.as<uint32_t>();
+  b.keys = ctx->keys64[0].as<unsigned long long>();
+  b.vals = ctx->vals[0].as<uint32_t>();
+  b.box_cap = ctx->box_cap;
+  b.rep_cap = ctx->rep_cap;
+  b.scene_cap = ctx->scene_cap;
+  return b;
+}
+
+int ensure_box_buffers(stq_context *ctx, int64_t box_cap) {
+  const size_t n = size_t(std::max<int64_t>(box_cap, 1));
+  STQ_CUDA(ctx, ctx->counts.ensure(sizeof(uint32_t) * n), "allocate replica counts");
+  STQ_CUDA(ctx, ctx->offsets.ensure(sizeof(uint32_t) * n), "allocate replica offsets");
+  STQ_CUDA(ctx, ctx->scan_ws.ensure(scan_workspace_bytes(int64_t(n))), "allocate scan workspace");
+  ctx->box_cap = int64_t(n);
+  return STQ_OK;
+}
+
+int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap) {
+  const size_t r = size_t(std::max<int64_t>(rep_cap, 1));
+  for (int b = 0; b < 2; ++b) {
+    STQ_CUDA(ctx, ctx->keys64[b].ensure(sizeof(unsigned long long) * r), "allocate keys");
+    STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * r), "allocate values");
+  }
+  STQ_CUDA(ctx, ctx->sort_ws.ensure(std::max(radix_workspace_bytes(int64_t(r), 8, 8),
+                                              radix_workspace_bytes(int64_t(r), 8, 4))),
+           "allocate sort workspace");
+  const size_t slots = r + size_t(cells_cap) + 1 + kSortedPad;
+  STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
+  ctx->rep_cap = int64_t(r);
+  ctx->slot_cap = int64_t(slots);
+  return STQ_OK;
+}
+
+int bits_for(int64_t v) {
+  int b = 0;
+  while ((int64_t(1) << b) < v) ++b;
+  return b;
+}
+
+// Statistics, axis, grid and replica counts: everything before the sort.
+int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b) {
+  stage_begin(ctx, kAxis);
+  STQ_CUDA(ctx, launch_batch_stats(ctx->stream, b), "launch batch statistics");
+  STQ_CUDA(ctx, launch_batch_policy(ctx->stream, b), "launch batch policy");
+  stage_end(ctx, kAxis);
+  stage_begin(ctx, kKeys);
+  STQ_CUDA(ctx, launch_batch_counts(ctx->stream, b), "launch replica counts");
+  STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.counts, b.offsets, ctx->box_cap, ctx->scan_ws.ptr,
+                                   &b.hdr->replicas, &ctx->launches),
+           "launch replica scan");
+  ctx->launches += 5;
+  return STQ_OK;
+}
+
+// Keys, sort, sentinels and gather.
+int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int cell_bits) {
+  STQ_CUDA(ctx, launch_batch_emit(ctx->stream, b), "launch replica emit");
+  stage_end(ctx, kKeys);
+  unsigned long long *kb[2] = {ctx->keys64[0].as<unsigned long long>(),
+                               ctx->keys64[1].as<unsigned long long>()};
+  uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
+  int which = 0;
+  stage_begin(ctx, kSort);
+  const int rbits = ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
+  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, ctx->rep_cap, 0, 32 + cell_bits,
+                                    ctx->sort_ws.ptr, &which, &ctx->launches, &b.hdr->replicas,
+                                    rbits),
+           "launch radix sort");
+  stage_end(ctx, kSort);
+  ctx->scene.sx = ctx->sx.as<float2>();
+  ctx->scene.syz = ctx->syz.as<float4>();
+  ctx->scene.sv = ctx->sv.as<int4>();
+  ctx->scene.sflag = ctx->sflag.as<int>();
+  stage_begin(ctx, kGather);
+  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, b.hdr, ctx->slot_cap),
+           "launch sentinel fill");
+  STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, ctx->rep_cap,
+                                    b.cell_base, b.scenes, ctx->scene),
+           "launch gather");
+  stage_end(ctx, kGather);
+  ctx->launches += 3;
+  return STQ_OK;
+}
+
+// Prepares a batch with exact buffer sizes (one synchronisation after the
+// replica count). Leaves the batch header read back in ctx->h_hdr.
+int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_off, int S,
+                  const int *axes, int axis) {
+  ctx->prepared = false;
+  const int64_t N = box_off[S];
+  const int64_t T = tiles_for(box_off, S);
+  STQ_TRY(ensure_staging(ctx, std::max(S, 1), int(std::max<int64_t>(T, 1))));
+  STQ_TRY(ensure_box_buffers(ctx, N));
+  fill_staging(ctx, box_off, S, axes, axis, nullptr, nullptr, nullptr);
+  STQ_TRY(upload_staging(ctx));
+  BatchBuffers b = batch_buffers(ctx, d_boxes);
+  STQ_TRY(enqueue_prepare_front(ctx, b));
+  STQ_TRY(read_header(ctx));
+  const int64_t R = ctx->h_hdr->replicas, cells = ctx->h_hdr->cells;
+  if (R + cells + 1 + kSortedPad > int64_t(INT32_MAX))
+    return fail(ctx, STQ_ERR_NO_MEMORY, "too many cell replicas for 32-bit positions");
+  STQ_TRY(ensure_replica_buffers(ctx, std::max(R, ctx->rep_cap), cells));
+  b = batch_buffers(ctx, d_boxes);
+  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(cells)));
+  ctx->n_scenes = S;
+  ctx->n_boxes = N;
+  ctx->length = R + cells - 1;
+  ctx->scene.length = ctx->length;
+  ctx->prepared = true;
+  return STQ_OK;
+}
+
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
               long long capacity, bool count_mode) {
+  BatchHeader *hdr = dev_hdr(ctx);
   SweepParams p;
   p.sx = ctx->scene.sx;
   p.syz = ctx->scene.syz;
   p.sv = ctx->scene.sv;
   p.begin = int32_t(begin);
-  p.end = int32_t(end);
+  p.end = int32_t(std::min<int64_t>(end, INT32_MAX));
   // start positions per work grab: at least ~4 grabs per resident warp
-  const int64_t span = end - begin;
+  const int64_t span = std::min<int64_t>(end, ctx->slot_cap) - begin;
   const int64_t want = int64_t(ctx->num_sms) * 64 * 4;
-  int64_t chunk = ((span / want) + 31) / 32 * 32;
+  const int64_t chunk = ((std::max<int64_t>(span, 0) / want) + 31) / 32 * 32;
   p.chunk = int32_t(chunk < 32 ? 32 : (chunk > ctx->tuning.chunk ? ctx->tuning.chunk : chunk));
   p.pairs = pairs;
   p.capacity = capacity;
-  DevScalars *ds = ctx->scalars.as<DevScalars>();
-  p.count = &ds->count;
-  p.work = &ds->work;
+  p.count = &hdr->pairs;
+  p.work = &hdr->work;
   p.box_counts = ctx->box_counts.as<int32_t>();
-  p.scell = ctx->scene.scell;
-  p.grid = ctx->scene.scell ? &ctx->prep.as<PrepInfo>()->grid : nullptr;
-  reset_sweep_kernel<<<1, 1, 0, ctx->stream>>>(ds);
-  STQ_CUDA(ctx, cudaGetLastError(), "reset sweep counters");
+  p.sflag = ctx->scene.sflag;
+  p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
+  p.hdr = hdr;
+  STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
   stage_begin(ctx, count_mode ? kCountSweep : kSweep);
-  STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms),
-           "launch sweep");
+  STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
   stage_end(ctx, count_mode ? kCountSweep : kSweep);
-  ctx->launches += (end > begin) ? 2 : 1;
+  ctx->launches += 2;
   return STQ_OK;
 }
 
@@ -228,15 +487,12 @@ int stq_context_create(int device, void *stream, stq_context **out) {
   ctx->stream = static_cast<cudaStream_t>(stream);
   DeviceGuard g(device);
   cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
-  if (cudaMallocHost(&ctx->h_scalars, sizeof(DevScalars)) != cudaSuccess ||
-      cudaMallocHost(&ctx->h_prep, sizeof(PrepInfo)) != cudaSuccess ||
-      ctx->scalars.ensure(sizeof(DevScalars)) != cudaSuccess ||
-      ctx->stats.ensure(sizeof(SceneStats)) != cudaSuccess ||
-      ctx->prep.ensure(sizeof(PrepInfo)) != cudaSuccess) {
+  apply_options(ctx);
+  if (cudaMallocHost(&ctx->h_hdr, sizeof(BatchHeader)) != cudaSuccess ||
+      ctx->aux.ensure(sizeof(BatchHeader)) != cudaSuccess || ensure_staging(ctx, 1, 1) != STQ_OK) {
     stq_context_destroy(ctx);
     return STQ_ERR_NO_MEMORY;
   }
-  apply_options(ctx);
   *out = ctx;
   return STQ_OK;
 }
@@ -247,17 +503,18 @@ void stq_context_destroy(stq_context *ctx) {
     DeviceGuard g(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     else cudaDeviceSynchronize();
-    for (DevBuf *b : {&ctx->sx, &ctx->syz, &ctx->sv, &ctx->keys[0], &ctx->keys[1],
-                      &ctx->vals[0], &ctx->vals[1], &ctx->sort_ws, &ctx->scalars,
-                      &ctx->partials, &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0],
-                      &ctx->pair_keys[1], &ctx->e2e_boxes, &ctx->e2e_pairs})
+    if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+    if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
+    if (ctx->graph_event) cudaEventDestroy(ctx->graph_event);
+    for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
+                      &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag,
+                      &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
+                      &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux})
       b->release();
-    ctx->e2e_mesh.release();
-    for (DevBuf *b : {&ctx->stats, &ctx->prep, &ctx->counts, &ctx->offsets, &ctx->scan_ws,
-                      &ctx->keys64[0], &ctx->keys64[1], &ctx->scell})
-      b->release();
-    if (ctx->h_scalars) cudaFreeHost(ctx->h_scalars);
-    if (ctx->h_prep) cudaFreeHost(ctx->h_prep);
+    if (ctx->in_host) cudaFreeHost(ctx->in_host);
+    if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
+    if (ctx->h_scene_pairs) cudaFreeHost(ctx->h_scene_pairs);
     for (int st = 0; st < kStages; ++st)
       for (int k = 0; k < 2; ++k)
         if (ctx->ev[st][k]) cudaEventDestroy(ctx->ev[st][k]);
@@ -272,7 +529,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 6 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 8 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -295,6 +552,12 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
     case STQ_OPT_CELL_SCALE:
       if (value > 64) return fail(ctx, STQ_ERR_INVALID_ARG, "cell scale: 1..64");
       break;
+    case STQ_OPT_REPLICA_BUDGET:
+      if (value > 64) return fail(ctx, STQ_ERR_INVALID_ARG, "replica budget: 1..64");
+      break;
+    case STQ_OPT_GRAPH:
+      if (value > 2) return fail(ctx, STQ_ERR_INVALID_ARG, "graph: 0 (default), 1 on, 2 off");
+      break;
     default:
       break;
   }
@@ -304,13 +567,15 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 6) return -1;
+  if (!ctx || option < 1 || option > 8) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
     case STQ_OPT_BLOCK_SIZE: return ctx->tuning.block;
-    case STQ_OPT_RADIX_BITS: return ctx->radix_bits;
+    case STQ_OPT_RADIX_BITS: return ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
     case STQ_OPT_CELL_SCALE: return int64_t(ctx->cell_scale);
+    case STQ_OPT_REPLICA_BUDGET: return ctx->budget;
+    case STQ_OPT_GRAPH: return ctx->options[STQ_OPT_GRAPH] == 2 ? 2 : 1;
     default: return ctx->options[option];
   }
 }
@@ -321,199 +586,108 @@ const char *stq_context_last_error(const stq_context *ctx) {
 
 int64_t stq_context_launch_count(const stq_context *ctx) { return ctx ? ctx->launches : -1; }
 
-}  // extern "C"
-
-namespace {
-
-int enqueue_build(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
-                  const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
-                  float inflation_radius, stq_aabb *d_boxes) {
+int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
+                    const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
+                    float inflation_radius, stq_aabb *d_boxes) {
+  if (!ctx) return STQ_ERR_INVALID_ARG;
   if (nV < 0 || nE < 0 || nF < 0 || nV + nE + nF > kMaxBoxes)
     return fail(ctx, STQ_ERR_INVALID_ARG, "box counts out of range");
   if ((nV > 0 && (!d_V0 || !d_V1)) || (nE > 0 && !d_E) || (nF > 0 && !d_F) ||
       (nV + nE + nF > 0 && !d_boxes))
     return fail(ctx, STQ_ERR_INVALID_ARG, "null buffer");
-  const float r_up = ref_next_up(inflation_radius);
-  DevScalars *ds = ctx->scalars.as<DevScalars>();
-  init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, 0);
-  STQ_CUDA(ctx, cudaGetLastError(), "init counters");
+  if (nV + nE + nF == 0) return STQ_OK;
+  DeviceGuard g(ctx->device);
+  BatchHeader *aux = ctx->aux.as<BatchHeader>();
+  STQ_CUDA(ctx, cudaMemsetAsync(aux, 0, sizeof(BatchHeader), ctx->stream), "clear flags");
   stage_begin(ctx, kBuild);
-  STQ_CUDA(ctx, launch_build_boxes(ctx->stream, d_V0, d_V1, nV, d_E, nE, d_F, nF, r_up,
-                                   d_boxes, &ds->flags),
+  STQ_CUDA(ctx, launch_build_boxes(ctx->stream, d_V0, d_V1, nV, d_E, nE, d_F, nF,
+                                   ref_next_up(inflation_radius), d_boxes, &aux->flags),
            "launch box build");
   stage_end(ctx, kBuild);
-  ctx->launches += (nV + nE + nF > 0) ? 2 : 1;
-  return STQ_OK;
+  ctx->launches += 1;
+  return read_header(ctx, aux);
 }
 
-}  // namespace
+int stq_batch_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1,
+                          const int64_t *h_vert_off, const int32_t *d_E, const int64_t *h_edge_off,
+                          const int32_t *d_F, const int64_t *h_face_off, int n_scenes,
+                          float inflation_radius, stq_aabb *d_boxes, int64_t *h_box_off) {
+  if (!ctx || n_scenes < 0 || !h_vert_off || !h_edge_off || !h_face_off || !h_box_off)
+    return STQ_ERR_INVALID_ARG;
+  std::vector<int64_t> box_off(size_t(n_scenes) + 1, 0);
+  for (int s = 0; s < n_scenes; ++s) {
+    const int64_t nv = h_vert_off[s + 1] - h_vert_off[s], ne = h_edge_off[s + 1] - h_edge_off[s],
+                  nf = h_face_off[s + 1] - h_face_off[s];
+    if (nv < 0 || ne < 0 || nf < 0) return fail(ctx, STQ_ERR_INVALID_ARG, "decreasing mesh offsets");
+    box_off[size_t(s) + 1] = box_off[size_t(s)] + nv + ne + nf;
+  }
+  const int64_t N = box_off[size_t(n_scenes)];
+  if (N > kMaxBoxes) return fail(ctx, STQ_ERR_INVALID_ARG, "too many boxes");
+  if (N > 0 && (!d_V0 || !d_V1 || !d_boxes)) return fail(ctx, STQ_ERR_INVALID_ARG, "null buffer");
+  std::copy(box_off.begin(), box_off.end(), h_box_off);
+  if (N == 0) return STQ_OK;
+  DeviceGuard g(ctx->device);
+  ctx->prepared = false;  // the staging block is reused
+  STQ_TRY(ensure_staging(ctx, std::max(n_scenes, 1),
+                         int(std::max<int64_t>(tiles_for(box_off.data(), n_scenes), 1))));
+  fill_staging(ctx, box_off.data(), n_scenes, nullptr, STQ_AXIS_AUTO, h_vert_off, h_edge_off,
+               h_face_off);
+  STQ_TRY(upload_staging(ctx));
+  stage_begin(ctx, kBuild);
+  STQ_CUDA(ctx, launch_batch_build(ctx->stream, d_V0, d_V1, dev_at<long long>(ctx, ctx->layout.voff),
+                                   d_E, dev_at<long long>(ctx, ctx->layout.eoff), d_F,
+                                   dev_at<long long>(ctx, ctx->layout.foff),
+                                   dev_at<long long>(ctx, ctx->layout.box_off), dev_hdr(ctx), N,
+                                   ref_next_up(inflation_radius), d_boxes),
+           "launch batched box build");
+  stage_end(ctx, kBuild);
+  ctx->launches += 1;
+  return read_header(ctx);
+}
 
-extern "C" {
-
-int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
-                    const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
-                    float inflation_radius, stq_aabb *d_boxes) {
+int stq_batch_prepare(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box_off,
+                      int n_scenes, const int *h_axis, int axis) {
   if (!ctx) return STQ_ERR_INVALID_ARG;
+  if (n_scenes < 1 || !h_box_off) return fail(ctx, STQ_ERR_INVALID_ARG, "no scenes");
+  if (h_box_off[0] != 0) return fail(ctx, STQ_ERR_INVALID_ARG, "box offsets must start at 0");
+  for (int s = 0; s < n_scenes; ++s) {
+    if (h_box_off[s + 1] < h_box_off[s]) return fail(ctx, STQ_ERR_INVALID_ARG, "decreasing box offsets");
+    const int a = h_axis ? h_axis[s] : axis;
+    if (a < STQ_AXIS_AUTO || a > STQ_AXIS_Z) return fail(ctx, STQ_ERR_INVALID_ARG, "axis");
+  }
+  if (h_box_off[n_scenes] > kMaxBoxes) return fail(ctx, STQ_ERR_INVALID_ARG, "too many boxes");
+  if (h_box_off[n_scenes] > 0 && !d_boxes) return fail(ctx, STQ_ERR_INVALID_ARG, "null boxes");
   DeviceGuard g(ctx->device);
-  const int st = enqueue_build(ctx, d_V0, d_V1, nV, d_E, nE, d_F, nF, inflation_radius, d_boxes);
-  if (st != STQ_OK) return st;
-  return read_scalars(ctx);
-}
-
-int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int *axis_out) {
-  if (!ctx || !axis_out || n < 0 || (n > 0 && !d_boxes)) return STQ_ERR_INVALID_ARG;
-  DeviceGuard g(ctx->device);
-  const int nb = axis_partial_blocks(n);
-  STQ_CUDA(ctx, ctx->partials.ensure(sizeof(double) * 6 * nb), "allocate axis partials");
-  DevScalars *ds = ctx->scalars.as<DevScalars>();
-  init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, 0);
-  STQ_CUDA(ctx, launch_axis_select(ctx->stream, d_boxes, n, ctx->partials.as<double>(), nb,
-                                   &ds->axis),
-           "launch axis selection");
-  ctx->launches += 3;
-  int st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  *axis_out = ctx->h_scalars->axis;
-  return STQ_OK;
+  return prepare_exact(ctx, d_boxes, h_box_off, n_scenes, h_axis, axis);
 }
 
 int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis) {
   if (!ctx) return STQ_ERR_INVALID_ARG;
   if (n < 0 || n > kMaxBoxes) return fail(ctx, STQ_ERR_INVALID_ARG, "box count out of range");
-  if (n > 0 && !d_boxes) return fail(ctx, STQ_ERR_INVALID_ARG, "null boxes");
-  if (axis < STQ_AXIS_AUTO || axis > STQ_AXIS_Z) return fail(ctx, STQ_ERR_INVALID_ARG, "axis");
+  const int64_t off[2] = {0, n};
+  return stq_batch_prepare(ctx, d_boxes, off, 1, nullptr, axis);
+}
+
+int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int *axis_out) {
+  if (!ctx || !axis_out || n < 0 || (n > 0 && !d_boxes)) return STQ_ERR_INVALID_ARG;
   DeviceGuard g(ctx->device);
-  ctx->prepared = false;
-  DevScalars *ds = ctx->scalars.as<DevScalars>();
-  PrepInfo *pi = ctx->prep.as<PrepInfo>();
-  init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, axis < 0 ? 0 : axis);
-  STQ_CUDA(ctx, cudaGetLastError(), "init counters");
-  ctx->launches += 1;
-  // 1. statistics, sweep axis and cell grid (device), read back once
-  STQ_CUDA(ctx, ctx->partials.ensure(stats_partials_bytes(n)), "allocate statistics");
-  stage_begin(ctx, kAxis);
-  STQ_CUDA(ctx, launch_scene_stats(ctx->stream, d_boxes, n, ctx->partials.as<double>(),
-                                   ctx->stats.as<SceneStats>(), &ds->flags),
-           "launch scene statistics");
-  STQ_CUDA(ctx, launch_grid_policy(ctx->stream, ctx->partials.as<double>(), n,
-                                   ctx->stats.as<SceneStats>(), axis,
-                                   int(ctx->options[STQ_OPT_CELLS]), ctx->cell_scale, &pi->grid,
-                                   &ds->axis),
-           "launch grid policy");
-  stage_end(ctx, kAxis);
-  ctx->launches += 3;
-  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_prep, pi, sizeof(PrepInfo), cudaMemcpyDeviceToHost,
-                                ctx->stream),
-           "read back grid");
-  int st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  const GridParams grid = ctx->h_prep->grid;
-  const size_t nn = size_t(n > 0 ? n : 1);
-
-  if (grid.ncells <= 1) {
-    // 2a. one cell: 32-bit keys, the sort of the reference's create_ds path
-    const size_t slots = size_t(n) + 1 + kSortedPad;
-    STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
-    STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
-    STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
-    for (int b = 0; b < 2; ++b) {
-      STQ_CUDA(ctx, ctx->keys[b].ensure(sizeof(uint32_t) * nn), "allocate sort keys");
-      STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * nn), "allocate sort values");
-    }
-    STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(n, 4, ctx->radix_bits)),
-             "allocate sort workspace");
-    uint32_t *kb[2] = {ctx->keys[0].as<uint32_t>(), ctx->keys[1].as<uint32_t>()};
-    uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
-    stage_begin(ctx, kKeys);
-    STQ_CUDA(ctx, launch_prep_keys(ctx->stream, d_boxes, n, &ds->axis, kb[0], vb[0], &ds->flags),
-             "launch key preparation");
-    stage_end(ctx, kKeys);
-    ctx->launches += n > 0 ? 1 : 0;
-    int which = 0;
-    stage_begin(ctx, kSort);
-    STQ_CUDA(ctx, radix_sort_u32(ctx->stream, kb, vb, n, ctx->radix_bits, ctx->sort_ws.ptr,
-                                 &which, &ctx->launches),
-             "launch radix sort");
-    stage_end(ctx, kSort);
-    ctx->scene.sx = ctx->sx.as<float2>();
-    ctx->scene.syz = ctx->syz.as<float4>();
-    ctx->scene.sv = ctx->sv.as<int4>();
-    ctx->scene.scell = nullptr;
-    ctx->scene.length = n;
-    stage_begin(ctx, kGather);
-    STQ_CUDA(ctx, launch_gather(ctx->stream, d_boxes, vb[which], n, &ds->axis, ctx->scene),
-             "launch gather");
-    stage_end(ctx, kGather);
-    ctx->launches += 1;
-    ctx->n = n;
-    ctx->prepared = true;
-    return STQ_OK;
-  }
-
-  // 2b. cells: replicate each box into the cells it touches
-  STQ_CUDA(ctx, ctx->counts.ensure(sizeof(uint32_t) * nn), "allocate replica counts");
-  STQ_CUDA(ctx, ctx->offsets.ensure(sizeof(uint32_t) * nn), "allocate replica offsets");
-  STQ_CUDA(ctx, ctx->scan_ws.ensure(scan_workspace_bytes(n)), "allocate scan workspace");
-  stage_begin(ctx, kKeys);
-  STQ_CUDA(ctx, launch_replica_count(ctx->stream, d_boxes, n, &pi->grid,
-                                     ctx->counts.as<uint32_t>()),
-           "launch replica count");
-  STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, ctx->counts.as<uint32_t>(),
-                                   ctx->offsets.as<uint32_t>(), n, ctx->scan_ws.ptr,
-                                   &pi->replicas, &ctx->launches),
-           "launch replica scan");
-  ctx->launches += 1;
-  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_prep, pi, sizeof(PrepInfo), cudaMemcpyDeviceToHost,
-                                ctx->stream),
-           "read back replica count");
-  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
-  const int64_t R = ctx->h_prep->replicas;
-  if (R < n || R + grid.ncells + 1 + kSortedPad > int64_t(INT32_MAX))
-    return fail(ctx, STQ_ERR_NO_MEMORY, "too many cell replicas for 32-bit positions");
-  const size_t slots = size_t(R) + size_t(grid.ncells) + 1 + kSortedPad;
-  STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
-  STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
-  STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
-  STQ_CUDA(ctx, ctx->scell.ensure(sizeof(int) * slots), "allocate sorted scene");
-  for (int b = 0; b < 2; ++b) {
-    STQ_CUDA(ctx, ctx->keys64[b].ensure(sizeof(unsigned long long) * size_t(R)), "allocate keys");
-    STQ_CUDA(ctx, ctx->vals[b].ensure(sizeof(uint32_t) * size_t(R)), "allocate values");
-  }
-  STQ_CUDA(ctx, ctx->sort_ws.ensure(radix_workspace_bytes(R, 8, 8)), "allocate sort workspace");
-  unsigned long long *kb[2] = {ctx->keys64[0].as<unsigned long long>(),
-                               ctx->keys64[1].as<unsigned long long>()};
-  uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
-  STQ_CUDA(ctx, launch_replica_emit(ctx->stream, d_boxes, n, &pi->grid,
-                                    ctx->offsets.as<uint32_t>(), kb[0], vb[0]),
-           "launch replica emit");
-  stage_end(ctx, kKeys);
-  ctx->launches += 1;
-  int which = 0;
-  stage_begin(ctx, kSort);
-  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, R, 0, 32 + grid.cell_bits,
-                                    ctx->sort_ws.ptr, &which, &ctx->launches),
-           "launch radix sort");
-  stage_end(ctx, kSort);
-  ctx->scene.sx = ctx->sx.as<float2>();
-  ctx->scene.syz = ctx->syz.as<float4>();
-  ctx->scene.sv = ctx->sv.as<int4>();
-  ctx->scene.scell = ctx->scell.as<int>();
-  ctx->scene.length = R + grid.ncells;
-  stage_begin(ctx, kGather);
-  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, int64_t(slots)),
-           "launch sentinel fill");
-  STQ_CUDA(ctx, launch_gather_cells(ctx->stream, d_boxes, kb[which], vb[which], R, &pi->grid,
-                                    ctx->scene),
-           "launch gather");
-  stage_end(ctx, kGather);
-  ctx->launches += 2;
-  ctx->n = n;
-  ctx->prepared = true;
+  ctx->prepared = false;  // the batch buffers are reused
+  const int64_t off[2] = {0, n};
+  STQ_TRY(ensure_staging(ctx, 1, int(std::max<int64_t>(tiles_for(off, 1), 1))));
+  STQ_TRY(ensure_box_buffers(ctx, n));
+  fill_staging(ctx, off, 1, nullptr, STQ_AXIS_AUTO, nullptr, nullptr, nullptr);
+  STQ_TRY(upload_staging(ctx));
+  BatchBuffers b = batch_buffers(ctx, d_boxes);
+  STQ_CUDA(ctx, launch_batch_stats(ctx->stream, b), "launch statistics");
+  STQ_CUDA(ctx, launch_batch_policy(ctx->stream, b), "launch policy");
+  ctx->launches += 5;
+  STQ_TRY(read_header(ctx));
+  *axis_out = ctx->h_hdr->axis;
   return STQ_OK;
 }
 
 int64_t stq_prepared_length(const stq_context *ctx) {
-  return (ctx && ctx->prepared) ? ctx->scene.length : -1;
+  return (ctx && ctx->prepared) ? ctx->length : -1;
 }
 
 int stq_sweep_prepared(stq_context *ctx, int64_t start, int64_t max_start, stq_pair *d_pairs,
@@ -522,47 +696,45 @@ int stq_sweep_prepared(stq_context *ctx, int64_t start, int64_t max_start, stq_p
   if (!ctx->prepared) return fail(ctx, STQ_ERR_NOT_PREPARED, "call stq_prepare first");
   if (!count || !next_start || capacity < 0 || (capacity > 0 && !d_pairs))
     return fail(ctx, STQ_ERR_INVALID_ARG, "null output or negative capacity");
-  const int64_t length = ctx->scene.length;
+  const int64_t length = ctx->length;
   if (start < 0 || start > length) return fail(ctx, STQ_ERR_INVALID_ARG, "start out of range");
   DeviceGuard g(ctx->device);
   const int64_t end = (max_start <= 0 || start + max_start > length) ? length : start + max_start;
-  int st = run_sweep(ctx, start, end, d_pairs, capacity, false);
-  if (st != STQ_OK) return st;
-  st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  const int64_t found = int64_t(ctx->h_scalars->count);
+  STQ_TRY(run_sweep(ctx, start, end, d_pairs, capacity, false));
+  STQ_TRY(read_header(ctx));
+  const int64_t found = int64_t(ctx->h_hdr->pairs);
   if (total) *total = found;
   if (found <= capacity) {
     *count = found;
     *next_start = end;
     return STQ_OK;
   }
-  // Overflow: count pairs per start box, keep the longest prefix that fits,
-  // and emit exactly that prefix again.
+  // Overflow: count pairs per start position, keep the longest prefix that
+  // fits, and emit exactly that prefix again.
   const int64_t m = end - start;
   STQ_CUDA(ctx, ctx->box_counts.ensure(sizeof(int32_t) * size_t(m)), "allocate box counts");
-  STQ_CUDA(ctx, ctx->prefix_ws.ensure(prefix_workspace_bytes(m)), "allocate prefix workspace");
+  STQ_CUDA(ctx, ctx->prefix_ws.ensure(prefix_workspace_bytes(m) + sizeof(DevScalars)),
+           "allocate prefix workspace");
   STQ_CUDA(ctx, cudaMemsetAsync(ctx->box_counts.ptr, 0, sizeof(int32_t) * size_t(m), ctx->stream),
            "clear box counts");
-  st = run_sweep(ctx, start, end, nullptr, 0, true);
-  if (st != STQ_OK) return st;
+  STQ_TRY(run_sweep(ctx, start, end, nullptr, 0, true));
+  DevScalars *sel = reinterpret_cast<DevScalars *>(ctx->prefix_ws.as<char>() + prefix_workspace_bytes(m));
   STQ_CUDA(ctx, launch_prefix_select(ctx->stream, ctx->box_counts.as<int32_t>(), m, capacity,
-                                     ctx->prefix_ws.ptr, ctx->scalars.as<DevScalars>(),
-                                     &ctx->launches),
+                                     ctx->prefix_ws.ptr, sel, &ctx->launches),
            "launch prefix selection");
-  st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  const int64_t prefix = ctx->h_scalars->prefix;
+  DevScalars h_sel;
+  STQ_CUDA(ctx, cudaMemcpyAsync(&h_sel, sel, sizeof(DevScalars), cudaMemcpyDeviceToHost, ctx->stream),
+           "read back prefix");
+  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  const int64_t prefix = h_sel.prefix;
   if (prefix <= 0) {
     *count = 0;
     *next_start = start;
     return fail(ctx, STQ_ERR_CAPACITY, "the first start box has more pairs than capacity");
   }
-  st = run_sweep(ctx, start, start + prefix, d_pairs, capacity, false);
-  if (st != STQ_OK) return st;
-  st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  *count = int64_t(ctx->h_scalars->count);
+  STQ_TRY(run_sweep(ctx, start, start + prefix, d_pairs, capacity, false));
+  STQ_TRY(read_header(ctx));
+  *count = int64_t(ctx->h_hdr->pairs);
   *next_start = start + prefix;
   if (*count > capacity) return fail(ctx, STQ_ERR_CUDA, "prefix re-sweep exceeded capacity");
   return STQ_OVERFLOW;
@@ -571,9 +743,149 @@ int stq_sweep_prepared(stq_context *ctx, int64_t start, int64_t max_start, stq_p
 int stq_sweep(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis, int64_t start,
               int64_t max_start, stq_pair *d_pairs, int64_t capacity, int64_t *count,
               int64_t *next_start, int64_t *total) {
-  int st = stq_prepare(ctx, d_boxes, n, axis);
-  if (st != STQ_OK) return st;
+  STQ_TRY(stq_prepare(ctx, d_boxes, n, axis));
   return stq_sweep_prepared(ctx, start, max_start, d_pairs, capacity, count, next_start, total);
+}
+
+int stq_batch_scene_pairs(stq_context *ctx, int64_t *h_counts, int n_scenes) {
+  if (!ctx || !h_counts || n_scenes < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx->prepared) return fail(ctx, STQ_ERR_NOT_PREPARED, "nothing prepared");
+  if (n_scenes > ctx->n_scenes) return fail(ctx, STQ_ERR_INVALID_ARG, "more scenes than prepared");
+  DeviceGuard g(ctx->device);
+  STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_scene_pairs, ctx->scene_pairs.ptr,
+                                sizeof(unsigned long long) * size_t(n_scenes), cudaMemcpyDeviceToHost,
+                                ctx->stream),
+           "read back scene counts");
+  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  for (int s = 0; s < n_scenes; ++s) h_counts[s] = int64_t(ctx->h_scene_pairs[s]);
+  return STQ_OK;
+}
+
+int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V1,
+                         const int64_t *h_vert_off, const int32_t *d_E, const int64_t *h_edge_off,
+                         const int32_t *d_F, const int64_t *h_face_off, int n_scenes,
+                         float inflation_radius, int axis, stq_pair *d_pairs, int64_t capacity,
+                         int64_t *count, int64_t *total, int64_t *h_scene_pairs) {
+  if (!ctx) return STQ_ERR_INVALID_ARG;
+  if (n_scenes < 1 || !h_vert_off || !h_edge_off || !h_face_off || !count || capacity < 0 ||
+      (capacity > 0 && !d_pairs) || axis < STQ_AXIS_AUTO || axis > STQ_AXIS_Z)
+    return fail(ctx, STQ_ERR_INVALID_ARG, "invalid batch arguments");
+  std::vector<int64_t> box_off(size_t(n_scenes) + 1, 0);
+  for (int s = 0; s < n_scenes; ++s) {
+    const int64_t nv = h_vert_off[s + 1] - h_vert_off[s], ne = h_edge_off[s + 1] - h_edge_off[s],
+                  nf = h_face_off[s + 1] - h_face_off[s];
+    if (nv < 0 || ne < 0 || nf < 0) return fail(ctx, STQ_ERR_INVALID_ARG, "decreasing mesh offsets");
+    box_off[size_t(s) + 1] = box_off[size_t(s)] + nv + ne + nf;
+  }
+  const int64_t N = box_off[size_t(n_scenes)];
+  if (N > kMaxBoxes / 8) return fail(ctx, STQ_ERR_INVALID_ARG, "too many boxes for one batch");
+  if (N > 0 && (!d_V0 || !d_V1)) return fail(ctx, STQ_ERR_INVALID_ARG, "null mesh");
+  DeviceGuard g(ctx->device);
+  // capacities: replicas within the budget, cells within the policy's cap
+  const int64_t T = std::max<int64_t>(tiles_for(box_off.data(), n_scenes), 1);
+  const int64_t rep_cap = std::max<int64_t>(int64_t(ctx->budget) * N, 1);
+  const int64_t cells_cap = N / 16 + n_scenes + 1;
+  STQ_TRY(ensure_staging(ctx, n_scenes, int(T)));
+  STQ_TRY(ensure_box_buffers(ctx, N));
+  STQ_TRY(ensure_replica_buffers(ctx, rep_cap, cells_cap));
+  STQ_CUDA(ctx, ctx->batch_boxes.ensure(sizeof(stq_aabb) * size_t(std::max<int64_t>(N, 1))),
+           "allocate batch boxes");
+  fill_staging(ctx, box_off.data(), n_scenes, nullptr, axis, h_vert_off, h_edge_off, h_face_off);
+  const stq_aabb *boxes = ctx->batch_boxes.as<stq_aabb>();
+  const int cell_bits = bits_for(cells_cap);
+  auto enqueue_all = [&]() -> int {
+    STQ_TRY(upload_staging(ctx));
+    stage_begin(ctx, kBuild);
+    STQ_CUDA(ctx, launch_batch_build(ctx->stream, d_V0, d_V1, dev_at<long long>(ctx, ctx->layout.voff),
+                                     d_E, dev_at<long long>(ctx, ctx->layout.eoff), d_F,
+                                     dev_at<long long>(ctx, ctx->layout.foff),
+                                     dev_at<long long>(ctx, ctx->layout.box_off), dev_hdr(ctx),
+                                     ctx->box_cap, ref_next_up(inflation_radius),
+                                     ctx->batch_boxes.as<stq_aabb>()),
+             "launch batched box build");
+    stage_end(ctx, kBuild);
+    const BatchBuffers b = batch_buffers(ctx, boxes);
+    STQ_TRY(enqueue_prepare_front(ctx, b));
+    STQ_TRY(enqueue_prepare_back(ctx, b, cell_bits));
+    STQ_TRY(run_sweep(ctx, 0, ctx->slot_cap, d_pairs, capacity, false));
+    STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_hdr, dev_hdr(ctx), sizeof(BatchHeader),
+                                  cudaMemcpyDeviceToHost, ctx->stream),
+             "read back batch header");
+    STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_scene_pairs, ctx->scene_pairs.ptr,
+                                  sizeof(unsigned long long) * size_t(n_scenes),
+                                  cudaMemcpyDeviceToHost, ctx->stream),
+             "read back scene counts");
+    ctx->launches += 1;
+    return STQ_OK;
+  };
+  const bool use_graph = ctx->options[STQ_OPT_GRAPH] != 2;
+  if (use_graph) {
+    if (!ctx->graph_stream) {
+      STQ_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->graph_stream, cudaStreamNonBlocking),
+               "create graph stream");
+      STQ_CUDA(ctx, cudaEventCreateWithFlags(&ctx->graph_event, cudaEventDisableTiming),
+               "create graph event");
+    }
+    // order after the caller's stream, then run on the private stream
+    STQ_CUDA(ctx, cudaEventRecord(ctx->graph_event, ctx->stream), "record caller event");
+    STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->graph_stream, ctx->graph_event, 0), "wait caller event");
+    cudaStream_t caller = ctx->stream;
+    ctx->stream = ctx->graph_stream;
+    GraphKey key;
+    const void *ptrs[6] = {d_V0, d_V1, d_E, d_F, d_pairs, boxes};
+    std::memcpy(key.ptr, ptrs, sizeof ptrs);
+    const int64_t sizes[8] = {ctx->box_cap, ctx->rep_cap, ctx->slot_cap, ctx->scene_cap,
+                              ctx->tile_cap, capacity, n_scenes, cell_bits};
+    std::memcpy(key.sizes, sizes, sizeof sizes);
+    for (int o = 0; o < 9; ++o) key.opts[o] = ctx->options[o];
+    key.opts[9] = int64_t(inflation_radius * 1e9f);
+    key.stream = caller;
+    int st = STQ_OK;
+    if (!ctx->graph || !(key == ctx->graph_key)) {
+      if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+      ctx->graph = nullptr;
+      cudaGraph_t graph = nullptr;
+      ctx->capturing = true;
+      cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+      st = e == cudaSuccess ? enqueue_all() : fail(ctx, STQ_ERR_CUDA, "begin graph capture", e);
+      cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &graph);
+      ctx->capturing = false;
+      if (st == STQ_OK && e2 != cudaSuccess) st = fail(ctx, STQ_ERR_CUDA, "end graph capture", e2);
+      if (st == STQ_OK) {
+        e = cudaGraphInstantiate(&ctx->graph, graph, 0);
+        if (e != cudaSuccess) st = fail(ctx, STQ_ERR_CUDA, "graph instantiate", e);
+      }
+      if (graph) cudaGraphDestroy(graph);
+      if (st == STQ_OK) ctx->graph_key = key;
+    }
+    if (st == STQ_OK) {
+      const cudaError_t e = cudaGraphLaunch(ctx->graph, ctx->stream);
+      if (e != cudaSuccess) st = fail(ctx, STQ_ERR_CUDA, "graph launch", e);
+    }
+    ctx->stream = caller;
+    if (st != STQ_OK) return st;
+    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->graph_stream), "synchronise graph stream");
+  } else {
+    STQ_TRY(enqueue_all());
+  }
+  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+  collect_stages(ctx);
+  const BatchHeader &h = *ctx->h_hdr;
+  if (h.flags & kFlagNaN) return fail(ctx, STQ_ERR_INVALID_INPUT, "a box bound is NaN");
+  if (h.flags & kFlagBadIndex) return fail(ctx, STQ_ERR_INVALID_INPUT, "an edge or face vertex index is out of range");
+  if (h.flags & kFlagReplicaOverflow)
+    return fail(ctx, STQ_ERR_NO_MEMORY, "cell replicas exceed the replica buffers");
+  ctx->n_scenes = n_scenes;
+  ctx->n_boxes = N;
+  ctx->length = int64_t(h.length);
+  ctx->scene.length = ctx->length;
+  ctx->prepared = true;
+  if (h_scene_pairs)
+    for (int s = 0; s < n_scenes; ++s) h_scene_pairs[s] = int64_t(ctx->h_scene_pairs[s]);
+  const int64_t found = int64_t(h.pairs);
+  if (total) *total = found;
+  *count = std::min(found, capacity);
+  return found <= capacity ? STQ_OK : STQ_OVERFLOW;
 }
 
 int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n, int axis,
@@ -655,16 +967,14 @@ int stq_broadphase_host(stq_context *ctx, const double *h_V0, const double *h_V1
   }
   if (be) STQ_CUDA(ctx, cudaMemcpyAsync(base + oE, h_E, be, cudaMemcpyHostToDevice, ctx->stream), "copy E");
   if (bf) STQ_CUDA(ctx, cudaMemcpyAsync(base + oF, h_F, bf, cudaMemcpyHostToDevice, ctx->stream), "copy F");
-  int st = enqueue_build(ctx, reinterpret_cast<const double *>(base),
-                         reinterpret_cast<const double *>(base + oV1), nV,
-                         reinterpret_cast<const int32_t *>(base + oE), nE,
-                         reinterpret_cast<const int32_t *>(base + oF), nF, inflation_radius,
-                         ctx->e2e_boxes.as<stq_aabb>());
-  if (st != STQ_OK) return st;
-  st = stq_prepare(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis);
-  if (st != STQ_OK) return st;
+  STQ_TRY(stq_build_boxes(ctx, reinterpret_cast<const double *>(base),
+                          reinterpret_cast<const double *>(base + oV1), nV,
+                          reinterpret_cast<const int32_t *>(base + oE), nE,
+                          reinterpret_cast<const int32_t *>(base + oF), nF, inflation_radius,
+                          ctx->e2e_boxes.as<stq_aabb>()));
+  STQ_TRY(stq_prepare(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis));
   int64_t next = 0;
-  st = stq_sweep_prepared(ctx, 0, 0, ctx->e2e_pairs.as<stq_pair>(), capacity, count, &next, total);
+  const int st = stq_sweep_prepared(ctx, 0, 0, ctx->e2e_pairs.as<stq_pair>(), capacity, count, &next, total);
   if (st != STQ_OK && st != STQ_OVERFLOW) return st;
   if (*count > 0) {
     STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, ctx->e2e_pairs.ptr, sizeof(stq_pair) * size_t(*count),
@@ -710,14 +1020,13 @@ int stq_brute_force(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, stq_pa
       (capacity > 0 && !d_pairs))
     return STQ_ERR_INVALID_ARG;
   DeviceGuard g(ctx->device);
-  DevScalars *ds = ctx->scalars.as<DevScalars>();
-  init_scalars_kernel<<<1, 1, 0, ctx->stream>>>(ds, 0);
-  STQ_CUDA(ctx, launch_brute_force(ctx->stream, d_boxes, n, d_pairs, capacity, &ds->count),
+  BatchHeader *aux = ctx->aux.as<BatchHeader>();
+  STQ_CUDA(ctx, cudaMemsetAsync(aux, 0, sizeof(BatchHeader), ctx->stream), "clear counters");
+  STQ_CUDA(ctx, launch_brute_force(ctx->stream, d_boxes, n, d_pairs, capacity, &aux->pairs),
            "launch brute force");
-  ctx->launches += 2;
-  const int st = read_scalars(ctx);
-  if (st != STQ_OK) return st;
-  *count = int64_t(ctx->h_scalars->count);
+  ctx->launches += 1;
+  STQ_TRY(read_header(ctx, aux));
+  *count = int64_t(ctx->h_hdr->pairs);
   return *count > capacity ? STQ_OVERFLOW : STQ_OK;
 }
 

@@ -1,0 +1,517 @@
+// batch.cu - prepare kernels of the scene table: per-scene statistics, sweep
+// axis and cell grid, cell replicas with their sort keys, and the sorted-scene
+// gather with one NaN sentinel after every cell.
+//
+// Reference: create_ds (src/sweep.cu:125-161) and the axis choice of
+// calc_mean / calc_variance (src/sweep.cu:93-123); the reference sorts one
+// scene along x. Here every scene of a batch gets its own sweep axis and
+// y/z cell grid, all scenes' cells get global ids, and one sort orders every
+// replica by (cell, min on the sweep axis).
+//
+// All sizes are read from the BatchHeader on the device, so one captured
+// graph serves any batch within the buffer capacities.
+#include "stq_device.cuh"
+#include "stq_internal.h"
+
+namespace stq {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kItems = kTileBoxes / kBlock;
+constexpr int kHistBias = 40;  // extent bucket = binary exponent + 40
+constexpr int kSampleBoxes = 1024;
+
+__device__ __forceinline__ float key_float(uint32_t k) {
+  const uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+  return __uint_as_float(b);
+}
+
+__device__ __forceinline__ void axes_bc(int a, int &b, int &c) {
+  b = a == 0 ? 1 : 0;
+  c = a == 2 ? 1 : 2;
+}
+
+template <typename T>
+__device__ T block_sum(T v, T *red) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFullMask, v, o);
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  T t = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kBlock / 32; ++w) t += red[w];
+  return t;  // valid in thread 0
+}
+
+// ---- 0. reset the per-scene accumulators ------------------------------------------
+__global__ void __launch_bounds__(kBlock)
+batch_reset_kernel(SceneRecord *scenes, const SceneInput *__restrict__ inputs,
+                   unsigned long long *scene_pairs, BatchHeader *hdr) {
+  const int S = hdr->n_scenes;
+  for (int s = blockIdx.x * kBlock + threadIdx.x; s < S; s += gridDim.x * kBlock) {
+    SceneRecord &r = scenes[s];
+    r.axis_mode = inputs[s].axis_mode;
+    r.cells_opt = inputs[s].cells_opt;
+    r.cell_scale = inputs[s].cell_scale;
+    scene_pairs[s] = 0ull;
+    for (int k = 0; k < 3; ++k) {
+      r.s1[k] = 0.0;
+      r.s2[k] = 0.0;
+      r.lo_key[k] = 0xffffffffu;
+      r.hi_key[k] = 0u;
+    }
+    r.inverted = 0;
+    for (int l = 0; l < kGridLevels; ++l) r.level_reps[l] = 0ull;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    hdr->flags = 0;
+    hdr->replicas = 0;
+    hdr->cells = 0;
+    hdr->length = 0;
+    hdr->work = 0;
+    hdr->pairs = 0;
+    hdr->prefix = 0;
+  }
+}
+
+// ---- 1. statistics: one tile (one scene) per block ------------------------------
+__global__ void __launch_bounds__(kBlock)
+batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
+                   SceneRecord *scenes, BatchHeader *hdr) {
+  if (int(blockIdx.x) >= hdr->n_tiles) return;
+  const TileRec t = tiles[blockIdx.x];
+  double s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+  uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
+  bool inverted = false, nan = false;
+  for (int i = threadIdx.x; i < t.count; i += kBlock) {
+    const stq_aabb &b = boxes[t.begin + i];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const float l = b.min[k], h = b.max[k];
+      nan |= (l != l) | (h != h);
+      inverted |= l > h;
+      s1[k] += double(l) + double(h);
+      s2[k] += double(l) * double(l) + double(h) * double(h);
+      lo[k] = min(lo[k], float_key(l));
+      hi[k] = max(hi[k], float_key(h));
+    }
+  }
+  __shared__ double dred[kBlock / 32];
+  SceneRecord &r = scenes[t.scene];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double a = block_sum(s1[k], dred);
+    if (threadIdx.x == 0) atomicAdd(&r.s1[k], a);
+    const double c = block_sum(s2[k], dred);
+    if (threadIdx.x == 0) atomicAdd(&r.s2[k], c);
+    const uint32_t l = __reduce_min_sync(kFullMask, lo[k]);
+    const uint32_t h = __reduce_max_sync(kFullMask, hi[k]);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&r.lo_key[k], l);
+      atomicMax(&r.hi_key[k], h);
+    }
+  }
+  if (__any_sync(kFullMask, inverted) && (threadIdx.x & 31) == 0) atomicOr(&r.inverted, 1);
+  if (__any_sync(kFullMask, nan) && (threadIdx.x & 31) == 0) atomicOr(&hdr->flags, kFlagNaN);
+}
+
+__device__ int grid_side(float L, float h) {
+  if (!(L > 0.f) || !(h > 0.f) || !isfinite(L)) return 1;
+  const float s = ceilf(L / h);
+  return s > 2048.f ? 2048 : (s < 1.f ? 1 : int(s));
+}
+
+__device__ __forceinline__ int level_side(int base, int level) {
+  const int s = (base + (1 << level) - 1) >> level;
+  return s < 1 ? 1 : s;
+}
+
+// ---- 2. policy: one block per scene ---------------------------------------------
+// Sweep axis of largest corner variance (x, then y, preferred on ties, as
+// src/simulation.cu:630-635) unless fixed; level-0 cell side = cell_scale x
+// median box extent (from a strided sample of the scene's boxes), at most
+// 2048 cells per axis and at most max(1, n / 16) cells.
+__global__ void __launch_bounds__(kBlock)
+batch_policy_kernel(const stq_aabb *__restrict__ boxes, const long long *__restrict__ box_off,
+                    SceneRecord *scenes, BatchHeader *hdr) {
+  const int s = blockIdx.x;
+  if (s >= hdr->n_scenes) return;
+  SceneRecord &r = scenes[s];
+  const long long b0 = box_off[s], n = box_off[s + 1] - b0;
+  int axis = r.axis_mode;
+  if (axis < 0) {
+    double var[3];
+    const double m = n > 0 ? 2.0 * double(n) : 1.0;
+    for (int k = 0; k < 3; ++k) {
+      const double mean = r.s1[k] / m;
+      var[k] = r.s2[k] - m * mean * mean;
+    }
+    axis = 0;
+    if (var[1] > var[axis]) axis = 1;
+    if (var[2] > var[axis]) axis = 2;
+  }
+  int b, c;
+  axes_bc(axis, b, c);
+  __shared__ unsigned hist[2][64];
+  for (int i = threadIdx.x; i < 128; i += kBlock) (&hist[0][0])[i] = 0u;
+  __syncthreads();
+  const bool automatic = r.cells_opt == 0 && !r.inverted && n > 1;
+  if (automatic) {
+    const long long step = n > kSampleBoxes ? n / kSampleBoxes : 1;
+    for (long long i = threadIdx.x; i < kSampleBoxes && i * step < n; i += kBlock) {
+      const stq_aabb &x = boxes[b0 + i * step];
+      const int ax[2] = {b, c};
+      for (int q = 0; q < 2; ++q) {
+        const float ext = x.max[ax[q]] - x.min[ax[q]];
+        int bucket = 0;
+        if (ext > 0.f) {
+          int e;
+          frexpf(ext, &e);
+          bucket = min(63, max(1, e + kHistBias));
+        }
+        atomicAdd(&hist[q][bucket], 1u);
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  const float lob = key_float(r.lo_key[b]), hib = key_float(r.hi_key[b]);
+  const float loc = key_float(r.lo_key[c]), hic = key_float(r.hi_key[c]);
+  const float Lb = hib - lob, Lc = hic - loc;
+  int nb = 1, nc = 1;
+  if (r.cells_opt > 1 && !r.inverted && n > 1) {
+    nb = nc = r.cells_opt;
+  } else if (automatic) {
+    float w[2];
+    for (int q = 0; q < 2; ++q) {
+      unsigned total = 0, run = 0;
+      for (int k = 0; k < 64; ++k) total += hist[q][k];
+      w[q] = 0.f;
+      for (int k = 0; k < 64; ++k) {
+        run += hist[q][k];
+        if (2 * run >= total && total > 0) {
+          w[q] = k == 0 ? 0.f : 0.75f * exp2f(float(k - kHistBias));
+          break;
+        }
+      }
+    }
+    if (!(w[0] > 0.f)) w[0] = Lb / 1024.f;
+    if (!(w[1] > 0.f)) w[1] = Lc / 1024.f;
+    nb = grid_side(Lb, r.cell_scale * w[0]);
+    nc = grid_side(Lc, r.cell_scale * w[1]);
+    const long long max_cells = max(1ll, min(1ll << 20, n / 16));
+    while ((long long)nb * nc > max_cells) {
+      if (nb >= nc) nb = (nb + 1) / 2;
+      else nc = (nc + 1) / 2;
+    }
+  }
+  if (!(Lb > 0.f) || !isfinite(Lb)) nb = 1;
+  if (!(Lc > 0.f) || !isfinite(Lc)) nc = 1;
+  r.base_nb = nb;
+  r.base_nc = nc;
+  GridParams &g = r.grid;
+  g.axis = axis;
+  g.ob = lob;
+  g.oc = loc;
+  g.Lb = Lb;
+  g.Lc = Lc;
+  if (s == 0) hdr->axis = axis;
+}
+
+struct Range {
+  int b0, b1, c0, c1;
+};
+
+__device__ __forceinline__ Range cell_range(const stq_aabb &x, int a, float ob, float ib, int nb,
+                                            float oc, float ic, int nc) {
+  int b, c;
+  axes_bc(a, b, c);
+  Range r;
+  r.b0 = cell_coord(x.min[b], ob, ib, nb);
+  r.b1 = cell_coord(x.max[b], ob, ib, nb);
+  r.c0 = cell_coord(x.min[c], oc, ic, nc);
+  r.c1 = cell_coord(x.max[c], oc, ic, nc);
+  return r;
+}
+
+__device__ __forceinline__ float inv_side(int n, float L) { return n > 1 ? float(n) / L : 0.f; }
+
+// ---- 3. replicas per grid level, per scene ------------------------------------------
+__global__ void __launch_bounds__(kBlock)
+batch_levels_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
+                    SceneRecord *scenes, const BatchHeader *hdr) {
+  if (int(blockIdx.x) >= hdr->n_tiles) return;
+  const TileRec t = tiles[blockIdx.x];
+  SceneRecord &r = scenes[t.scene];
+  const GridParams g = r.grid;
+  int nbl[kGridLevels], ncl[kGridLevels];
+  float ibl[kGridLevels], icl[kGridLevels];
+#pragma unroll
+  for (int l = 0; l < kGridLevels; ++l) {
+    nbl[l] = level_side(r.base_nb, l);
+    ncl[l] = level_side(r.base_nc, l);
+    ibl[l] = inv_side(nbl[l], g.Lb);
+    icl[l] = inv_side(ncl[l], g.Lc);
+  }
+  unsigned long long reps[kGridLevels] = {};
+  for (int i = threadIdx.x; i < t.count; i += kBlock) {
+    const stq_aabb &x = boxes[t.begin + i];
+#pragma unroll
+    for (int l = 0; l < kGridLevels; ++l) {
+      const Range q = cell_range(x, g.axis, g.ob, ibl[l], nbl[l], g.oc, icl[l], ncl[l]);
+      reps[l] += (unsigned long long)(q.b1 - q.b0 + 1) * (unsigned long long)(q.c1 - q.c0 + 1);
+    }
+  }
+  __shared__ unsigned long long red[kBlock / 32];
+#pragma unroll
+  for (int l = 0; l < kGridLevels; ++l) {
+    const unsigned long long v = block_sum(reps[l], red);
+    if (threadIdx.x == 0) atomicAdd(&r.level_reps[l], v);
+  }
+}
+
+// ---- 4. choose the finest level within the replica budget; cell bases ----------
+__global__ void __launch_bounds__(1024)
+batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
+                    unsigned int *cell_base, BatchHeader *hdr) {
+  __shared__ unsigned int warp_tot[32];
+  __shared__ unsigned int carry;
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  const int S = hdr->n_scenes;
+  const long long budget = hdr->budget;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int base = 0; base < S; base += 1024) {
+    const int s = base + threadIdx.x;
+    unsigned int cells = 0;
+    if (s < S) {
+      SceneRecord &r = scenes[s];
+      const long long n = box_off[s + 1] - box_off[s];
+      int level = kGridLevels;  // none fits: one cell
+      if (r.cells_opt > 1) {
+        level = 0;  // a requested grid is kept as is
+      } else {
+        for (int l = 0; l < kGridLevels; ++l)
+          if ((long long)r.level_reps[l] <= budget * n) {
+            level = l;
+            break;
+          }
+      }
+      GridParams &g = r.grid;
+      g.level = level;
+      g.nb = level < kGridLevels ? level_side(r.base_nb, level) : 1;
+      g.nc = level < kGridLevels ? level_side(r.base_nc, level) : 1;
+      g.ib = inv_side(g.nb, g.Lb);
+      g.ic = inv_side(g.nc, g.Lc);
+      if (g.ib == 0.f) g.nb = 1;
+      if (g.ic == 0.f) g.nc = 1;
+      g.ncells = g.nb * g.nc;
+      cells = unsigned(g.ncells);
+    }
+    // block exclusive scan of the cell counts
+    unsigned int x = cells;
+    for (int o = 1; o < 32; o <<= 1) {
+      const unsigned int y = __shfl_up_sync(kFullMask, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      unsigned int w = warp_tot[lane];
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int y = __shfl_up_sync(kFullMask, w, o);
+        if (lane >= o) w += y;
+      }
+      warp_tot[lane] = w;
+    }
+    __syncthreads();
+    const unsigned int excl = carry + (warp > 0 ? warp_tot[warp - 1] : 0u) + x - cells;
+    if (s < S) cell_base[s] = excl;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += warp_tot[31];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    cell_base[S] = carry;
+    hdr->cells = carry;
+  }
+}
+
+// ---- 5. per-box replica counts (zero past the last box, up to the capacity) -----
+__global__ void __launch_bounds__(kBlock)
+batch_count_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
+                   const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
+                   uint32_t *__restrict__ counts, long long box_cap) {
+  const long long N = hdr->n_boxes;
+  if (int(blockIdx.x) < hdr->n_tiles) {
+    const TileRec t = tiles[blockIdx.x];
+    const GridParams g = scenes[t.scene].grid;
+    for (int i = threadIdx.x; i < t.count; i += kBlock) {
+      const Range q = cell_range(boxes[t.begin + i], g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
+      counts[t.begin + i] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
+    }
+  }
+  // boxes past the batch contribute nothing to the scan
+  for (long long i = N + blockIdx.x * (long long)kBlock + threadIdx.x; i < box_cap;
+       i += (long long)gridDim.x * kBlock)
+    counts[i] = 0u;
+}
+
+// ---- 6. replica keys: (global cell id << 32) | order-preserving min --------------
+__global__ void __launch_bounds__(kBlock)
+batch_emit_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
+                  const SceneRecord *__restrict__ scenes, const unsigned int *__restrict__ cell_base,
+                  BatchHeader *hdr, const uint32_t *__restrict__ offsets,
+                  unsigned long long *__restrict__ keys, uint32_t *__restrict__ vals,
+                  long long rep_cap) {
+  const bool fits = (long long)hdr->replicas <= rep_cap;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    // on overflow of the replica buffers nothing is emitted or swept
+    // every cell is followed by its sentinel; the last one is not a start position
+    hdr->length = fits && hdr->cells > 0 ? hdr->replicas + hdr->cells - 1 : 0u;
+    if (!fits) {
+      atomicOr(&hdr->flags, kFlagReplicaOverflow);
+      hdr->replicas = 0;
+    }
+  }
+  if (!fits || int(blockIdx.x) >= hdr->n_tiles) return;
+  const TileRec t = tiles[blockIdx.x];
+  const GridParams g = scenes[t.scene].grid;
+  const unsigned long long cb0 = cell_base[t.scene];
+  for (int i = threadIdx.x; i < t.count; i += kBlock) {
+    const long long bi = t.begin + i;
+    const stq_aabb &x = boxes[bi];
+    const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
+    const unsigned long long xk = float_key(x.min[g.axis]);
+    uint32_t o = offsets[bi];
+    for (int cb = q.b0; cb <= q.b1; ++cb)
+      for (int cc = q.c0; cc <= q.c1; ++cc) {
+        keys[o] = ((cb0 + (unsigned long long)(cb * g.nc + cc)) << 32) | xk;
+        vals[o] = uint32_t(bi);
+        ++o;
+      }
+  }
+}
+
+__global__ void __launch_bounds__(kBlock)
+fill_sentinels_kernel(float2 *__restrict__ sx, const BatchHeader *hdr, int64_t slots_cap) {
+  const int64_t slots = min(slots_cap, int64_t(hdr->length) + 1 + kSortedPad);
+  const float q = __int_as_float(0x7fc00000);
+  for (int64_t k = blockIdx.x * int64_t(kBlock) + threadIdx.x; k < slots;
+       k += int64_t(gridDim.x) * kBlock)
+    sx[k] = make_float2(q, q);
+}
+
+// Sorted replica p of global cell c goes to position p + c: every cell is
+// followed by one NaN slot, which ends every x-run at the cell boundary.
+// sflag of a position: bit 0 set if the cell is the box's first cell along b,
+// bit 1 if it is its first cell along c, scene index above. Since the cell
+// coordinate is monotone, the cell of a pair's reference point (max of the
+// two minima on b, on c) is the max of the two boxes' first cells; both boxes
+// lie in this cell, so the reference point is here exactly when, on each of
+// b and c, one of the two replicas is its box's first cell.
+__global__ void __launch_bounds__(kBlock)
+gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long *__restrict__ keys,
+                    const uint32_t *__restrict__ order, const BatchHeader *hdr,
+                    const unsigned int *__restrict__ cell_base,
+                    const SceneRecord *__restrict__ scenes, float2 *__restrict__ sx,
+                    float4 *__restrict__ syz, int4 *__restrict__ sv, int *__restrict__ sflag) {
+  const int64_t R = hdr->replicas;
+  const int S = hdr->n_scenes;
+  for (int64_t p = blockIdx.x * int64_t(kBlock) + threadIdx.x; p < R;
+       p += int64_t(gridDim.x) * kBlock) {
+    const unsigned int cell = unsigned(keys[p] >> 32);
+    const uint32_t bi = order[p];
+    int lo = 0, hi = S - 1;  // scene of the cell
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (cell_base[mid] <= cell) lo = mid;
+      else hi = mid - 1;
+    }
+    const GridParams g = scenes[lo].grid;
+    int b, c;
+    axes_bc(g.axis, b, c);
+    const stq_aabb &x = boxes[bi];
+    const int local = int(cell - cell_base[lo]);
+    const int cb = local / g.nc, cc = local - cb * g.nc;
+    const int fb = cell_coord(x.min[b], g.ob, g.ib, g.nb) == cb;
+    const int fc = cell_coord(x.min[c], g.oc, g.ic, g.nc) == cc;
+    const int64_t k = p + cell;
+    sx[k] = make_float2(x.min[g.axis], x.max[g.axis]);
+    syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
+    sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
+    sflag[k] = (lo << 2) | (fc << 1) | fb;
+  }
+}
+
+int blocks_for(int64_t n, int cap = 152 * 16) {
+  int64_t g = (n + kBlock - 1) / kBlock;
+  return int(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+__global__ void __launch_bounds__(kBlock)
+reset_sweep_kernel(BatchHeader *hdr, unsigned long long *scene_pairs) {
+  const int S = hdr->n_scenes;
+  for (int s = blockIdx.x * kBlock + threadIdx.x; s < S; s += gridDim.x * kBlock)
+    scene_pairs[s] = 0ull;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    hdr->pairs = 0ull;
+    hdr->work = 0;
+  }
+}
+
+}  // namespace
+
+cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long long *scene_pairs,
+                               int scene_cap) {
+  reset_sweep_kernel<<<blocks_for(scene_cap, 64), kBlock, 0, s>>>(hdr, scene_pairs);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_stats(cudaStream_t s, const BatchBuffers &b) {
+  batch_reset_kernel<<<blocks_for(b.scene_cap, 64), kBlock, 0, s>>>(b.scenes, b.inputs,
+                                                                      b.scene_pairs, b.hdr);
+  batch_stats_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b) {
+  batch_policy_kernel<<<unsigned(b.scene_cap), kBlock, 0, s>>>(b.boxes, b.box_off, b.scenes, b.hdr);
+  batch_levels_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr);
+  batch_choose_kernel<<<1, 1024, 0, s>>>(b.box_off, b.scenes, b.cell_base, b.hdr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b) {
+  batch_count_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr,
+                                                             b.counts, b.box_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b) {
+  batch_emit_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.cell_base,
+                                                            b.hdr, b.offsets, b.keys, b.vals,
+                                                            b.rep_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, const BatchHeader *hdr,
+                                  int64_t slots_cap) {
+  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(sx, hdr, slots_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
+                                const unsigned long long *keys, const uint32_t *order,
+                                const BatchHeader *hdr, int64_t rep_cap,
+                                const unsigned int *cell_base, const SceneRecord *scenes,
+                                SortedScene scene) {
+  gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
+                                                             scenes, scene.sx, scene.syz, scene.sv,
+                                                             scene.sflag);
+  return cudaGetLastError();
+}
+
+}  // namespace stq

@@ -28,7 +28,8 @@ int64_t num_tiles(int64_t n, int tile) { return (n + tile - 1) / tile; }
 template <typename K, int BITS>
 __global__ void __launch_bounds__(kSortBlock)
 upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift,
-               uint32_t *__restrict__ hist, int64_t ntiles) {
+               uint32_t *__restrict__ hist, int64_t ntiles, const unsigned int *d_n) {
+  if (d_n && int64_t(*d_n) < n) n = *d_n;
   constexpr int BINS = 1 << BITS;
   constexpr int TILE = TileShape<K>::tile;
   __shared__ uint32_t h[kSortWarps][BINS];
@@ -108,7 +109,9 @@ __global__ void __launch_bounds__(kSortBlock)
 downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
                  const uint32_t *__restrict__ vin, uint32_t *__restrict__ vout,
                  int64_t n, int shift, const uint32_t *__restrict__ tile_off,
-                 const uint32_t *__restrict__ digit_base, int64_t ntiles) {
+                 const uint32_t *__restrict__ digit_base, int64_t ntiles,
+                 const unsigned int *d_n) {
+  if (d_n && int64_t(*d_n) < n) n = *d_n;
   constexpr int BINS = 1 << BITS;
   constexpr int ITEMS = TileShape<K>::items;
   constexpr int TILE = TileShape<K>::tile;
@@ -182,7 +185,7 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
     }
   }
   __syncthreads();
-  const int count = int(n - tile_start < TILE ? n - tile_start : TILE);
+  const int count = int(n - tile_start < TILE ? (n > tile_start ? n - tile_start : 0) : TILE);
   for (int p = threadIdx.x; p < count; p += kSortBlock) {
     const int d = stage_d[p];
     kout[gbase[d] + (p - tile_prefix[d])] = stage[p];
@@ -204,7 +207,7 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
 template <typename K, int BITS, bool VALS>
 cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
                       int begin_bit, int end_bit, void *workspace, int *which,
-                      int64_t *launches) {
+                      int64_t *launches, const unsigned int *d_n = nullptr) {
   constexpr int BINS = 1 << BITS;
   constexpr int TILE = TileShape<K>::tile;
   *which = 0;
@@ -215,12 +218,12 @@ cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
   int cur = 0;
   for (int shift = begin_bit; shift < end_bit; shift += BITS) {
     upsweep_kernel<K, BITS><<<unsigned(ntiles), kSortBlock, 0, s>>>(kbuf[cur], n, shift,
-                                                                     hist, ntiles);
+                                                                     hist, ntiles, d_n);
     scan_rows_kernel<<<BINS, kSortBlock, 0, s>>>(hist, ntiles, totals);
     scan_totals_kernel<BINS><<<1, kSortBlock, 0, s>>>(totals);
     downsweep_kernel<K, BITS, VALS><<<unsigned(ntiles), kSortBlock, 0, s>>>(
         kbuf[cur], kbuf[cur ^ 1], VALS ? vbuf[cur] : nullptr,
-        VALS ? vbuf[cur ^ 1] : nullptr, n, shift, hist, totals, ntiles);
+        VALS ? vbuf[cur ^ 1] : nullptr, n, shift, hist, totals, ntiles, d_n);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (launches) *launches += 4;
@@ -255,9 +258,13 @@ cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2], int64_t 
 
 cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2], uint32_t *vbuf[2],
                                 int64_t n, int begin_bit, int end_bit, void *workspace,
-                                int *which, int64_t *launches) {
+                                int *which, int64_t *launches, const unsigned int *d_n,
+                                int bits) {
+  if (bits == 4)
+    return sort_impl<unsigned long long, 4, true>(s, kbuf, vbuf, n, begin_bit, end_bit,
+                                                  workspace, which, launches, d_n);
   return sort_impl<unsigned long long, 8, true>(s, kbuf, vbuf, n, begin_bit, end_bit,
-                                                workspace, which, launches);
+                                                workspace, which, launches, d_n);
 }
 
 // ---- exclusive scan of uint32 counts (reduce-then-scan, no waiting) -------------

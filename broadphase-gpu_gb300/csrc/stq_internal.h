@@ -48,6 +48,7 @@ struct DevScalars {
 enum : int {
   kFlagNaN = 1,        // a box bound is NaN
   kFlagBadIndex = 2,   // an edge or face index is outside [0, nV)
+  kFlagReplicaOverflow = 4,  // cell replicas exceed the replica buffers
 };
 
 // Cell grid on the two non-sweep axes b, c (the other two axes in increasing
@@ -59,19 +60,68 @@ struct GridParams {
   int axis;       // sweep axis a
   int nb, nc;     // cells along b and c
   int ncells;     // nb * nc
-  int cell_bits;  // bits of the largest cell id
-  int inverted;   // some box has min > max on b or c: cells disabled
   float ob, oc;   // grid origin on b and c
   float ib, ic;   // cells per unit length on b and c
+  float Lb, Lc;   // extent of the scene on b and c
+  int level;      // grid level chosen against the replica budget
+  int pad;
 };
 
-// Per-scene statistics gathered in one pass over the boxes.
-struct SceneStats {
-  unsigned int lo_key[3];   // order-preserving min of the minima
-  unsigned int hi_key[3];   // order-preserving max of the maxima
-  unsigned int hist[3][64]; // log2 histogram of the box extents
-  int inverted;             // some box has min > max
+constexpr int kGridLevels = 6;  // level L halves the base grid L times
+
+// One scene of a batch: inputs written by the host, the rest computed on the
+// device by the prepare kernels.
+struct SceneRecord {
+  // inputs
+  int axis_mode;        // -1: largest variance, else the axis
+  int cells_opt;        // 0 automatic, 1 no cells, k > 1 a k x k grid
+  float cell_scale;     // automatic cell side in median box extents
+  int pad0;
+  // statistics
+  double s1[3], s2[3];              // sum(min + max), sum(min^2 + max^2)
+  unsigned int lo_key[3], hi_key[3];  // order-preserving min / max bounds
+  unsigned int hist[3][64];         // log2 histogram of the extents
+  int inverted;                     // some box has min > max on an axis
+  int base_nb, base_nc;             // level-0 grid of the policy
+  int pad1;
+  unsigned long long level_reps[kGridLevels];  // replicas per grid level
+  // results
+  GridParams grid;
+};
+
+// Per-scene inputs written by the host (copied into the records on reset).
+struct SceneInput {
+  int axis_mode;
+  int cells_opt;
+  float cell_scale;
   int pad;
+};
+
+// Device-side header of a prepared batch: sizes read by every kernel, so a
+// captured graph can be replayed for any batch within its capacities.
+struct BatchHeader {
+  long long n_boxes;        // input: boxes in the batch
+  int n_scenes;             // input: scenes
+  int flags;                // kFlag* bits
+  unsigned int replicas;    // R, cell replicas
+  unsigned int cells;       // total cells of all scenes
+  unsigned int length;      // sweep positions: R + cells
+  int work;                 // sweep grab cursor
+  unsigned long long pairs; // pairs found by the last sweep
+  long long prefix;         // overflow: start positions of the prefix that fits
+  int axis;                 // sweep axis of scene 0
+  int budget;               // replica budget: replicas <= budget * boxes per scene
+  int n_tiles;              // input: entries of the tile table
+  int pad;
+};
+
+// A tile of at most kTileBoxes consecutive boxes of one scene (built by the
+// host from the scene offsets), so that a block reduces per-scene values once.
+constexpr int kTileBoxes = 4096;
+struct TileRec {
+  long long begin;  // first box of the tile
+  int count;        // boxes in the tile
+  int scene;        // scene of the tile
 };
 
 // Sweep-kernel tuning (autotuned or set through stq_context_set_option).
@@ -88,7 +138,7 @@ struct SortedScene {
   float2 *sx = nullptr;   // (min, max) on the sweep axis
   float4 *syz = nullptr;  // (min_b, min_c, max_b, max_c) on the other axes
   int4 *sv = nullptr;     // (vertexIds[0..2], id)
-  int *scell = nullptr;   // cell id of each position (cells mode)
+  int *sflag = nullptr;   // first-cell bits (0: along b, 1: along c), scene << 2
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
 
@@ -96,15 +146,16 @@ struct SweepParams {
   const float2 *sx;
   const float4 *syz;
   const int4 *sv;
-  int32_t begin, end;        // start positions [begin, end)
+  int32_t begin, end;        // start positions [begin, min(end, hdr->length))
   int32_t chunk;             // start positions per grab
   stq_pair *pairs;
   long long capacity;
   unsigned long long *count;
   int *work;
   int32_t *box_counts;       // count mode: pairs per start position (k - begin)
-  const int *scell;          // cells mode: cell id per position, else null
-  const GridParams *grid;    // cells mode: grid on the device
+  const int *sflag;          // first-cell bits and scene of each position
+  unsigned long long *scene_pairs;  // per-scene pair counters
+  const BatchHeader *hdr;    // device sizes (length bounds the sweep range)
 };
 
 // ---- launch wrappers (each returns the launch error) -------------------------
@@ -124,25 +175,44 @@ cudaError_t launch_gather(cudaStream_t s, const stq_aabb *boxes,
                           const uint32_t *order, int64_t n, const int *d_axis,
                           SortedScene scene);
 
-// ---- cells mode ------------------------------------------------------------------
-// stats: one pass; grid: policy kernel (mode: -1 auto axis, else the axis;
-// cells_opt: 0 automatic, 1 no cells, k > 1 a k x k grid; scale: cell side
-// in median box extents)
-size_t stats_partials_bytes(int64_t n);
-cudaError_t launch_scene_stats(cudaStream_t s, const stq_aabb *boxes, int64_t n,
-                               double *partials, SceneStats *stats, int *flags);
-cudaError_t launch_grid_policy(cudaStream_t s, const double *partials, int64_t n,
-                               const SceneStats *stats, int axis_mode, int cells_opt,
-                               float scale, GridParams *grid, int *d_axis);
-cudaError_t launch_replica_count(cudaStream_t s, const stq_aabb *boxes, int64_t n,
-                                 const GridParams *grid, uint32_t *counts);
-cudaError_t launch_replica_emit(cudaStream_t s, const stq_aabb *boxes, int64_t n,
-                                const GridParams *grid, const uint32_t *offsets,
-                                unsigned long long *keys, uint32_t *vals);
-cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, int64_t slots);
+// ---- batch prepare (scene table) ---------------------------------------------------
+// Buffers sized by host capacities; actual sizes come from the BatchHeader.
+struct BatchBuffers {
+  const stq_aabb *boxes;
+  const long long *box_off;     // n_scenes + 1 box offsets
+  const TileRec *tiles;         // n_tiles entries
+  int tile_cap;
+  const SceneInput *inputs;     // n_scenes entries
+  unsigned long long *scene_pairs;  // n_scenes pair counters
+  SceneRecord *scenes;
+  unsigned int *cell_base;      // n_scenes + 1
+  BatchHeader *hdr;
+  uint32_t *counts, *offsets;   // per box
+  unsigned long long *keys;     // replica keys (sort input)
+  uint32_t *vals;               // replica box indices (sort input)
+  long long box_cap;            // capacities
+  long long rep_cap;
+  int scene_cap;
+};
+cudaError_t launch_batch_stats(cudaStream_t s, const BatchBuffers &b);
+cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b);
+cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b);
+cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b);
+cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, const BatchHeader *hdr,
+                                  int64_t slots_cap);
 cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
-                                int64_t R, const GridParams *grid, SortedScene scene);
+                                const BatchHeader *hdr, int64_t rep_cap,
+                                const unsigned int *cell_base, const SceneRecord *scenes,
+                                SortedScene scene);
+// Batched box build: scene s has vertices [voff[s], voff[s+1]) etc.; box ids
+// are global (box_off[s] + local), vertex ids local to the scene.
+cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V1,
+                               const long long *voff, const int32_t *E, const long long *eoff,
+                               const int32_t *F, const long long *foff, const long long *box_off,
+                               BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out);
+cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long long *scene_pairs,
+                               int scene_cap);
 
 // LSD radix sort of (uint32 key, uint32 value) or (uint64 key) pairs.
 // kbuf/vbuf are double buffers; *which receives the buffer index holding the
@@ -156,11 +226,13 @@ cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2],
                            int *which, int64_t *launches);
 cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2],
                                 uint32_t *vbuf[2], int64_t n, int begin_bit, int end_bit,
-                                void *workspace, int *which, int64_t *launches);
+                                void *workspace, int *which, int64_t *launches,
+                                const unsigned int *d_n = nullptr, int bits = 8);
 // exclusive scan of n uint32 counts; *d_total receives the sum
 size_t scan_workspace_bytes(int64_t n);
 cudaError_t exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n,
                                void *workspace, uint32_t *d_total, int64_t *launches);
+
 
 cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p,
                          const SweepTuning &t, bool count_mode, int num_sms);

@@ -21,13 +21,27 @@ namespace stq {
 
 namespace {
 
-template <int G, int Q, int BLOCK, bool COUNT, bool CELLS>
+// Appends the warp's n staged pairs with one atomic; pairs past the capacity
+// are counted but not written.
+__device__ __forceinline__ void flush_staged(const int2 *st, int n, int lane, const SweepParams &p) {
+  unsigned long long base = 0;
+  if (lane == 0) base = atomicAdd(p.count, (unsigned long long)n);
+  base = __shfl_sync(kFullMask, base, 0);
+  int2 *out = reinterpret_cast<int2 *>(p.pairs);
+  for (int i = lane; i < n; i += 32)
+    if (base + i < (unsigned long long)p.capacity) out[base + i] = st[i];
+  __syncwarp();
+}
+
+template <int G, int Q, int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK)
 stq_sweep_kernel(const SweepParams p) {
   static_assert(32 % G == 0, "lane group must divide the warp");
   static_assert((Q & (Q - 1)) == 0 && Q >= 32, "queue depth: power of two >= 32");
   constexpr int E = 32 / G;  // lane groups per warp
+  constexpr int STAGE = 64;  // pairs staged per warp before one global append
   __shared__ int ring[BLOCK / 32][Q];
+  __shared__ int2 stage[COUNT ? 1 : BLOCK / 32][COUNT ? 1 : STAGE];
 
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;              // lane within group
@@ -46,14 +60,15 @@ stq_sweep_kernel(const SweepParams p) {
   float kmax = 0.f;
   float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
   int4 kv = make_int4(0, 0, 0, 0);
-  const int span = p.end - p.begin;
-  // cells mode: grid and the cell of the current start box
-  float gob = 0.f, goc = 0.f, gib = 0.f, gic = 0.f;
-  int gnb = 1, gnc = 1, kcb = 0, kcc = 0;
-  if (CELLS) {
-    const GridParams g = *p.grid;
-    gob = g.ob, goc = g.oc, gib = g.ib, gic = g.ic, gnb = g.nb, gnc = g.nc;
-  }
+  const int end = min(p.end, int(p.hdr->length));
+  const int span = end - p.begin;
+  int kf = 0;  // first-cell bits and scene of the current start box
+  // warp-uniform: staged pairs, and pairs of the current scene not yet added
+  // to its counter
+  int staged = 0;
+  int wscene = 0;
+  unsigned long long wpairs = 0;
+  int2 *st = stage[COUNT ? 0 : (threadIdx.x >> 5)];
 
   while (true) {
     // 1. Refill the ring with start boxes that have at least one candidate.
@@ -67,7 +82,7 @@ stq_sweep_kernel(const SweepParams p) {
           break;
         }
         next_k = p.begin + c;
-        chunk_end = min(next_k + p.chunk, p.end);
+        chunk_end = min(next_k + p.chunk, end);
       }
       const int take = min(32, min(Q - qsize, chunk_end - next_k));
       const int kk = next_k + lane;
@@ -92,11 +107,7 @@ stq_sweep_kernel(const SweepParams p) {
         kb = p.syz[k];
         kv = p.sv[k];
         acc = 0;
-        if (CELLS) {
-          const int cell = p.scell[k];
-          kcb = cell / gnc;
-          kcc = cell - kcb * gnc;
-        }
+        kf = p.sflag[k];
       }
     }
     qhead = (qhead + ntake) & (Q - 1);
@@ -119,26 +130,38 @@ stq_sweep_kernel(const SweepParams p) {
       const float4 b = p.syz[j];
       const int4 bv = p.sv[j];
       hit = overlap_bc(kb, b) && valid_pair(kv, bv) && !covertex(kv, bv);
-      // a pair shared by several cells is emitted only in the cell of its
-      // reference point (max of the minima on b and c)
-      if (CELLS && hit)
-        hit = cell_coord(fmaxf(kb.x, b.x), gob, gib, gnb) == kcb &&
-              cell_coord(fmaxf(kb.y, b.y), goc, gic, gnc) == kcc;
+      // a pair found in several cells is emitted only in the cell of its
+      // reference point: on b and on c, one of the two replicas must be its
+      // box's first cell (the candidate's bits are read only when needed)
+      if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j]) & 3) == 3;
       lo_id = min(kv.w, bv.w);
       hi_id = max(kv.w, bv.w);
     }
-    // 4. Emit: one global atomic per warp step.
+    // 4. Emit: compact the step's hits into the warp's staging buffer; append
+    //    it to the pair list with one global atomic per 32 or more pairs.
     const unsigned hm = __ballot_sync(kFullMask, hit);
+    const int ghits = __popc(hm & grp_mask);
     if (COUNT) {
-      acc += __popc(hm & grp_mask);
+      acc += ghits;
     } else if (hm) {
-      unsigned long long base = 0;
-      if (lane == 0) base = atomicAdd(p.count, (unsigned long long)__popc(hm));
-      base = __shfl_sync(kFullMask, base, 0);
-      if (hit) {
-        const unsigned long long idx = base + __popc(hm & lanemask_lt());
-        if (idx < (unsigned long long)p.capacity)
-          reinterpret_cast<int2 *>(p.pairs)[idx] = make_int2(lo_id, hi_id);
+      if (hit) st[staged + __popc(hm & lanemask_lt())] = make_int2(lo_id, hi_id);
+      staged += __popc(hm);
+      // per-scene counts: one register while the warp stays in one scene
+      const int lead = __shfl_sync(kFullMask, kf >> 2, __ffs(hm) - 1);
+      if (__all_sync(kFullMask, !hit || (kf >> 2) == lead)) {
+        if (lead != wscene) {
+          if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+          wscene = lead;
+          wpairs = 0;
+        }
+        wpairs += __popc(hm);
+      } else if (gl == 0 && ghits) {
+        atomicAdd(&p.scene_pairs[kf >> 2], (unsigned long long)ghits);
+      }
+      if (staged >= 32) {
+        __syncwarp();
+        flush_staged(st, staged, lane, p);
+        staged = 0;
       }
     }
     // 5. A group whose G lanes all passed continues; otherwise its run ended.
@@ -152,12 +175,17 @@ stq_sweep_kernel(const SweepParams p) {
       }
     }
   }
+  if (!COUNT) {
+    __syncwarp();
+    if (staged) flush_staged(st, staged, lane, p);
+    if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+  }
 }
 
-template <int G, int Q, int BLOCK, bool COUNT, bool CELLS>
+template <int G, int Q, int BLOCK, bool COUNT>
 cudaError_t launch_variant(cudaStream_t s, const SweepParams &p, int num_sms) {
   int per_sm = 0;
-  auto kern = stq_sweep_kernel<G, Q, BLOCK, COUNT, CELLS>;
+  auto kern = stq_sweep_kernel<G, Q, BLOCK, COUNT>;
   cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
@@ -173,8 +201,7 @@ cudaError_t launch_variant(cudaStream_t s, const SweepParams &p, int num_sms) {
 
 template <int G, int Q, int BLOCK>
 cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, int sms) {
-  return p.scell ? launch_variant<G, Q, BLOCK, false, true>(s, p, sms)
-                 : launch_variant<G, Q, BLOCK, false, false>(s, p, sms);
+  return launch_variant<G, Q, BLOCK, false>(s, p, sms);
 }
 
 template <int G, int Q>
@@ -307,8 +334,7 @@ cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p, const SweepTuning
                          bool count_mode, int num_sms) {
   if (p.end <= p.begin) return cudaSuccess;
   if (count_mode)  // per-start-box counts do not depend on the tuning
-    return p.scell ? launch_variant<8, 64, 256, true, true>(s, p, num_sms)
-                   : launch_variant<8, 64, 256, true, false>(s, p, num_sms);
+    return launch_variant<8, 64, 256, true>(s, p, num_sms);
   switch (t.lanes) {
     case 1: return launch_g<1>(s, p, t, num_sms);
     case 2: return launch_g<2>(s, p, t, num_sms);

@@ -42,6 +42,7 @@ STQ_ERR_NOT_PREPARED = -7
 
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
 OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
+OPT_REPLICA_BUDGET, OPT_GRAPH = 7, 8
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
@@ -75,6 +76,13 @@ ABI_SIGNATURES = {
     "stq_context_stage_times": (ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_double), _c_i64p,
                                                ctypes.c_int]),
     "stq_stage_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "stq_batch_build_boxes": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int,
+                                             ctypes.c_float, _vp, _vp]),
+    "stq_batch_prepare": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int]),
+    "stq_batch_scene_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int]),
+    "stq_batch_broadphase": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int,
+                                            ctypes.c_float, ctypes.c_int, _vp, ctypes.c_int64, _c_i64p,
+                                            _c_i64p, _vp]),
     "stq_sort_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "stq_brute_force": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p]),
 }
@@ -252,6 +260,45 @@ class Context:
         k = self.lib.stq_context_stage_times(self._h, ms, calls, 16)
         return {self.lib.stq_stage_name(i).decode(): (ms[i], calls[i]) for i in range(k)}
 
+    # -- batches of scenes ----------------------------------------------------
+    def batch_build_boxes(self, V0, V1, voff, E, eoff, F, foff, out,
+                          inflation_radius: float = 0.0) -> np.ndarray:
+        """Device meshes of several scenes (host offsets voff/eoff/foff, S+1 each)
+        -> boxes in `out`; returns the S+1 box offsets."""
+        S = len(voff) - 1
+        vo, eo, fo = (np.ascontiguousarray(x, np.int64) for x in (voff, eoff, foff))
+        bo = np.zeros(S + 1, np.int64)
+        self._check(self.lib.stq_batch_build_boxes(self._h, _ptr(V0), _ptr(V1), vo.ctypes.data, _ptr(E),
+                                                   eo.ctypes.data, _ptr(F), fo.ctypes.data, S,
+                                                   float(inflation_radius), _ptr(out), bo.ctypes.data))
+        return bo
+
+    def batch_prepare(self, boxes, box_off, axes=None, axis: int = AXIS_AUTO) -> None:
+        bo = np.ascontiguousarray(box_off, np.int64)
+        ax = None if axes is None else np.ascontiguousarray(axes, np.int32)
+        self._check(self.lib.stq_batch_prepare(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1,
+                                               None if ax is None else ax.ctypes.data, axis))
+
+    def batch_scene_pairs(self, n_scenes: int) -> np.ndarray:
+        out = np.zeros(n_scenes, np.int64)
+        self._check(self.lib.stq_batch_scene_pairs(self._h, out.ctypes.data, n_scenes))
+        return out
+
+    def batch_broadphase(self, V0, V1, voff, E, eoff, F, foff, pairs, capacity: int,
+                         axis: int = AXIS_AUTO, inflation_radius: float = 0.0):
+        """Fused batched pipeline (graph-captured unless OPT_GRAPH=2).
+        Returns (SweepResult, per-scene pair counts)."""
+        S = len(voff) - 1
+        vo, eo, fo = (np.ascontiguousarray(x, np.int64) for x in (voff, eoff, foff))
+        per = np.zeros(S, np.int64)
+        c, tot = ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_batch_broadphase(self._h, _ptr(V0), _ptr(V1), vo.ctypes.data, _ptr(E),
+                                           eo.ctypes.data, _ptr(F), fo.ctypes.data, S,
+                                           float(inflation_radius), axis, _ptr(pairs), capacity,
+                                           ctypes.byref(c), ctypes.byref(tot), per.ctypes.data)
+        self._check(st, allow=(STQ_OK, STQ_OVERFLOW))
+        return SweepResult(st, c.value, self.prepared_length, tot.value), per
+
     def sort_pairs(self, pairs, count: int) -> None:
         self._check(self.lib.stq_sort_pairs(self._h, _ptr(pairs), count))
 
@@ -338,3 +385,28 @@ def splitmix64(x: int) -> int:
     lib = load_scenes()
     lib.stq_splitmix64.restype = ctypes.c_uint64
     return int(lib.stq_splitmix64(ctypes.c_uint64(x)))
+
+
+def concat_meshes(meshes: list) -> tuple:
+    """Concatenates meshes into one batch: (V0, V1, E, F, voff, eoff, foff), with
+    vertex indices kept local to each scene."""
+    V0 = np.concatenate([m.V0 for m in meshes]) if meshes else np.zeros((0, 3))
+    V1 = np.concatenate([m.V1 for m in meshes]) if meshes else np.zeros((0, 3))
+    E = np.concatenate([m.E for m in meshes]) if meshes else np.zeros((0, 2), np.int32)
+    F = np.concatenate([m.F for m in meshes]) if meshes else np.zeros((0, 3), np.int32)
+    off = lambda k: np.concatenate([[0], np.cumsum([k(m) for m in meshes])]).astype(np.int64)  # noqa: E731
+    return (V0, V1, E, F, off(lambda m: m.V0.shape[0]), off(lambda m: m.E.shape[0]),
+            off(lambda m: m.F.shape[0]))
+
+
+def batch_scenes(n_scenes: int = 256, lo: float = 1e3, hi: float = 2e5, seed: int = 2) -> list:
+    """Cloth-pair scenes with box counts log-uniform in [lo, hi], sheet offset
+    U(0.002, 0.05) and motion sigma U(0.001, 0.01), per-scene seeds by splitmix64."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for s in range(n_scenes):
+        target = float(np.exp(rng.uniform(np.log(lo), np.log(hi))))
+        g = cloth_pair_grid_for(int(target))
+        out.append(cloth_pair(g=g, z_offset=float(rng.uniform(0.002, 0.05)), angle_deg=10.0,
+                              sigma=float(rng.uniform(0.001, 0.01)), seed=splitmix64(seed * 1000003 + s)))
+    return out

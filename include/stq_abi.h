@@ -88,8 +88,12 @@ typedef enum stq_option {
   STQ_OPT_CELLS = 4,           /* cell grid on the two non-sweep axes: 0 automatic,
                                   1 no cells (plain sweep), k > 1 a k x k grid      */
   STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
-  STQ_OPT_CELL_SCALE = 6       /* automatic cell side in median box extents (1..64,
+  STQ_OPT_CELL_SCALE = 6,      /* automatic cell side in median box extents (1..64,
                                   default 4)                                        */
+  STQ_OPT_REPLICA_BUDGET = 7,  /* cell replicas per box a scene may use (1..64,
+                                  default 4); finer grids beyond it are coarsened   */
+  STQ_OPT_GRAPH = 8            /* stq_batch_broadphase: 1 capture and replay a CUDA
+                                  graph (default), 2 plain stream launches          */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -118,7 +122,8 @@ int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1,
                     const int32_t *d_F, int64_t nF, float inflation_radius,
                     stq_aabb *d_boxes);
 
-/* Axis of largest variance of the box corners (0, 1 or 2). */
+/* Axis of largest variance of the box corners (0, 1 or 2). Reuses the batch
+ * buffers: a previously prepared scene must be prepared again. */
 int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
                     int *axis_out);
 
@@ -130,8 +135,8 @@ int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
 /* Number of sweep positions of the prepared scene: the start-box cursor of
  * stq_sweep_prepared runs over [0, length). Equal to the box count when
  * cells are off; with cells, boxes are replicated into the cells they touch
- * and every cell is followed by one empty position. -1 if nothing is
- * prepared. */
+ * and every cell but the last is followed by one empty position. -1 if
+ * nothing is prepared. */
 int64_t stq_prepared_length(const stq_context *ctx);
 
 /* Sweeps start boxes [start, start + max_start) of the prepared scene in
@@ -177,6 +182,50 @@ int stq_context_enable_timing(stq_context *ctx, int enable);
 int stq_context_stage_times(stq_context *ctx, double *ms, int64_t *calls,
                             int max_stages);
 const char *stq_stage_name(int stage);
+
+/* ---- batches of scenes (one launch sequence for many scenes) ----------------
+ * Scene s owns boxes [box_off[s], box_off[s+1]) of one box array. Every scene
+ * gets its own sweep axis and cell grid; cells of all scenes are sorted and
+ * swept together, and no pair crosses scenes. Pair ids are the boxes' `id`
+ * fields (batch-global when the boxes come from stq_batch_build_boxes). */
+
+/* Swept boxes of a batch of meshes. Scene s has vertices [h_vert_off[s],
+ * h_vert_off[s+1]) of d_V0/d_V1, edges [h_edge_off[s], ...) of d_E and faces
+ * [h_face_off[s], ...) of d_F, with vertex indices local to the scene. Boxes
+ * are written scene after scene (vertices, edges, faces of each); a box's id
+ * is its batch index, its vertex ids are local. h_box_off receives the
+ * n_scenes + 1 box offsets. Reuses the batch buffers: a previously prepared
+ * scene must be prepared again. */
+int stq_batch_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1,
+                          const int64_t *h_vert_off, const int32_t *d_E,
+                          const int64_t *h_edge_off, const int32_t *d_F,
+                          const int64_t *h_face_off, int n_scenes,
+                          float inflation_radius, stq_aabb *d_boxes,
+                          int64_t *h_box_off);
+
+/* Prepares a batch (h_axis: n_scenes axes, or NULL for one `axis` for all);
+ * stq_sweep_prepared then sweeps every scene of it. */
+int stq_batch_prepare(stq_context *ctx, const stq_aabb *d_boxes,
+                      const int64_t *h_box_off, int n_scenes, const int *h_axis,
+                      int axis);
+
+/* Pairs per scene found by the last sweep (n_scenes entries). */
+int stq_batch_scene_pairs(stq_context *ctx, int64_t *h_counts, int n_scenes);
+
+/* The whole batched pipeline on device meshes (build, prepare, sweep of all
+ * start boxes) with no host synchronisation until the end. With
+ * STQ_OPT_GRAPH = 1 the launch sequence is captured once as a CUDA graph and
+ * replayed for any later batch that fits the same capacities and buffers.
+ * Writes the pairs to d_pairs; *count = pairs written; h_scene_pairs (may be
+ * NULL) receives per-scene counts. STQ_OVERFLOW: more pairs than capacity
+ * (the first capacity pairs are written; call again with a larger buffer). */
+int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V1,
+                         const int64_t *h_vert_off, const int32_t *d_E,
+                         const int64_t *h_edge_off, const int32_t *d_F,
+                         const int64_t *h_face_off, int n_scenes,
+                         float inflation_radius, int axis, stq_pair *d_pairs,
+                         int64_t capacity, int64_t *count, int64_t *total,
+                         int64_t *h_scene_pairs);
 
 /* Sorts d_pairs[0..count) lexicographically on the device (deterministic
  * output order for callers that need one). */
