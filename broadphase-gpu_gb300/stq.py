@@ -83,6 +83,8 @@ ABI_SIGNATURES = {
     "stq_batch_broadphase": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, _vp, ctypes.c_int64, _c_i64p,
                                             _c_i64p, _vp]),
+    "stq_sweep_static": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int, _vp, ctypes.c_int64, _c_i64p,
+                                        _c_i64p, _vp]),
     "stq_sort_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
     "stq_brute_force": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _c_i64p]),
 }
