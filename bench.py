@@ -191,6 +191,49 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
             "batched_over_plain": t_plain / t_batch, "graph": True}
 
 
+def bench_serving(stq, local, n_requests, rate, seed=4):
+    """Poisson arrivals of time-stepped cloth-pair requests (boxes log-uniform
+    in [1e4, 2e6], 1-20 steps, step noise 0.003, HBM budget 160 GB): the
+    continuous-batching server against the same server run one request at a
+    time (serial). Latency = completion - arrival."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for k in range(n_requests):
+        n = float(np.exp(rng.uniform(np.log(1e4), np.log(2e6))))
+        m = stq.cloth_pair(g=stq.cloth_pair_grid_for(int(n)), z_offset=float(rng.uniform(0.002, 0.05)),
+                           sigma=float(rng.uniform(0.001, 0.01)), seed=stq.splitmix64(seed * 7919 + k))
+        reqs.append((m, int(rng.integers(1, 21)), k))
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
+    out = {}
+    for label, max_scenes in (("batched", 256), ("serial", 1)):
+        sv = stq.Server(local, None, budget_bytes=160 << 30, max_boxes=1 << 25, max_scenes=max_scenes)
+        t0 = time.perf_counter()
+        i, arrive, done = 0, {}, {}
+        while len(done) < n_requests:
+            now = time.perf_counter() - t0
+            while i < n_requests and arrivals[i] <= now:
+                m, steps, sd = reqs[i]
+                arrive[sv.submit(m, steps, 0.003, sd)] = arrivals[i]
+                i += 1
+            for rid in sv.tick():
+                done[rid] = time.perf_counter() - t0
+            st = sv.stats()
+            if st["active"] == 0 and st["queued"] == 0 and i < n_requests:
+                time.sleep(max(0.0, min(0.002, arrivals[i] - (time.perf_counter() - t0))))
+        elapsed = time.perf_counter() - t0
+        lat = np.array([done[r] - arrive[r] for r in done])
+        pairs = sum(int(sv.result(r)[0].sum()) for r in done)
+        box_steps = sum(m.num_boxes * s for m, s, _ in reqs)
+        out[label] = {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                      "pairs_per_s": pairs / elapsed, "box_steps_per_s": box_steps / elapsed,
+                      "seconds": elapsed, "ticks": sv.stats()["ticks"]}
+        sv.close()
+    return {"workload": f"{n_requests} Poisson requests at {rate} req/s; cloth pairs, boxes log-uniform "
+                        "in [1e4, 2e6], 1-20 steps, step noise 0.003; budget 160 GB", **out}
+
+
 def run_reference(args, w):
     import __graft_entry__ as entry
 
@@ -235,6 +278,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=48)
+    ap.add_argument("--serve-rate", type=float, default=100.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -283,6 +329,9 @@ def main():
     r = ctx.sweep_prepared(pairs, cap)
     cap = int(r.total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    # the project's autotuner picks cell scale, radix width, lane-group width,
+    # queue depth and block size for this workload (not timed)
+    tune_ms, tuned = ctx.autotune(boxes, [0, n], pairs, cap)
 
     def step():
         ctx.build_boxes(V0, V1, E, F, boxes)
@@ -345,7 +394,7 @@ def main():
         "data": "synthetic (seeded crumpled-sheet trajectories; the reference's mesh benchmarks are not distributed)",
         "config": {"workload": args.workload, "boxes": n, "vertices": nV, "edges": nE, "faces": nF,
                    "pairs": npairs, "axis": "max-variance", "l2": "flushed between steps (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "tuned": tuned},
         "pairs_per_s": world * npairs / (ms_per_step / 1e3),
         "stage_ms_per_step": {k: v[0] / args.steps for k, v in stages.items() if v[1]},
         "gpu_launches": launches,
@@ -384,6 +433,9 @@ def main():
 
     if not args.no_batch:
         line["batched"] = bench_batched(stq, torch, dev, stream, local, args.steps, args.warmup, flush)
+
+    if not args.no_serve and rank == 0:
+        line["serve"] = bench_serving(stq, local, args.serve_requests, args.serve_rate)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = entry.load_oracle()

@@ -21,7 +21,8 @@ CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 ROOT = PKG.parent
 
-CUDA_SOURCES = ["boxes.cu", "batch.cu", "radix_sort.cu", "sweep.cu", "abi.cu", "static_sweep.cu"]
+CUDA_SOURCES = ["boxes.cu", "batch.cu", "radix_sort.cu", "sweep.cu", "abi.cu", "server.cu", "static_sweep.cu",
+                "mesh_io.cpp"]
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_FLAGS = [
     GENCODE, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",

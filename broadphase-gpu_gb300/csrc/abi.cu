@@ -15,116 +15,21 @@
 #include <string>
 #include <vector>
 
-#include "stq_device.cuh"
-#include "stq_internal.h"
+#include <functional>
 
-using namespace stq;
+#include "context.h"
 
-constexpr int kStages = 8;
-const char *const kStageNames[kStages] = {"build", "axis", "keys", "sort",
-                                          "gather", "sweep", "count_sweep", "pair_sort"};
-enum Stage { kBuild, kAxis, kKeys, kSort, kGather, kSweep, kCountSweep, kPairSort };
+namespace stq {
+namespace ctxops {
 
-// Input block uploaded with one copy before every prepare: the batch header,
-// the scene offsets (boxes, and vertices/edges/faces for batched builds), the
-// per-scene options and the tile table. Offsets are fixed by the capacities.
-struct Staging {
-  int scene_cap = 0, tile_cap = 0;
-  size_t hdr = 0, box_off = 0, voff = 0, eoff = 0, foff = 0, inputs = 0, tiles = 0, total = 0;
-  static Staging make(int scene_cap, int tile_cap) {
-    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
-    Staging st;
-    st.scene_cap = scene_cap;
-    st.tile_cap = tile_cap;
-    size_t o = 0;
-    st.hdr = o, o = up(o + sizeof(BatchHeader));
-    const size_t offs = sizeof(long long) * size_t(scene_cap + 1);
-    st.box_off = o, o = up(o + offs);
-    st.voff = o, o = up(o + offs);
-    st.eoff = o, o = up(o + offs);
-    st.foff = o, o = up(o + offs);
-    st.inputs = o, o = up(o + sizeof(SceneInput) * size_t(scene_cap));
-    st.tiles = o, o = up(o + sizeof(TileRec) * size_t(tile_cap));
-    st.total = o;
-    return st;
-  }
-};
+DeviceGuard::DeviceGuard(int dev) {
+  if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) changed = cudaSetDevice(dev) == cudaSuccess;
+}
+DeviceGuard::~DeviceGuard() {
+  if (changed) cudaSetDevice(prev);
+}
 
-struct GraphKey {
-  const void *ptr[6] = {};
-  int64_t sizes[8] = {};
-  int64_t opts[10] = {};
-  cudaStream_t stream = nullptr;
-  bool operator==(const GraphKey &o) const {
-    return std::memcmp(ptr, o.ptr, sizeof ptr) == 0 && std::memcmp(sizes, o.sizes, sizeof sizes) == 0 &&
-           std::memcmp(opts, o.opts, sizeof opts) == 0 && stream == o.stream;
-  }
-};
-
-struct stq_context {
-  int device = 0;
-  int num_sms = 152;
-  cudaStream_t stream = nullptr;
-  std::string error;
-  int64_t launches = 0;
-  SweepTuning tuning;
-  int64_t options[16] = {};
-  float cell_scale = 2.f;
-  int budget = 4;
-
-  // capacities of the batch buffers
-  int scene_cap = 0, tile_cap = 0;
-  int64_t box_cap = 0, rep_cap = 0, slot_cap = 0;
-  Staging layout;
-  DevBuf in_dev;
-  char *in_host = nullptr;
-  size_t in_host_bytes = 0;
-  DevBuf scenes, cell_base, scene_pairs, counts, offsets, scan_ws, keys64[2], vals[2], sort_ws;
-  DevBuf sx, syz, sv, sflag, box_counts, prefix_ws, pair_keys[2];
-  DevBuf batch_boxes, e2e_boxes, e2e_pairs, e2e_mesh;
-  DevBuf aux;  // header of calls outside a batch (box build, all-pairs check)
-
-  // prepared batch (host view)
-  bool prepared = false;
-  int n_scenes = 0;
-  int64_t n_boxes = 0, length = 0;
-  SortedScene scene;
-  BatchHeader *h_hdr = nullptr;             // pinned readback
-  unsigned long long *h_scene_pairs = nullptr;  // pinned readback
-  int h_scene_pairs_cap = 0;
-
-  // captured graph of stq_batch_broadphase, on a private stream (the legacy
-  // default stream cannot be captured)
-  cudaStream_t graph_stream = nullptr;
-  cudaEvent_t graph_event = nullptr;
-  cudaGraphExec_t graph = nullptr;
-  GraphKey graph_key;
-  bool capturing = false;
-
-  // stage timers
-  bool timing = false;
-  cudaEvent_t ev[kStages][2] = {};
-  bool pending[kStages] = {};
-  double stage_ms[kStages] = {};
-  int64_t stage_calls[kStages] = {};
-};
-
-namespace {
-
-struct DeviceGuard {
-  int prev = -1;
-  bool changed = false;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
-      changed = cudaSetDevice(dev) == cudaSuccess;
-    }
-  }
-  ~DeviceGuard() {
-    if (changed) cudaSetDevice(prev);
-  }
-};
-
-int fail(stq_context *ctx, int status, const char *what, cudaError_t e = cudaSuccess) {
+int fail(stq_context *ctx, int status, const char *what, cudaError_t e) {
   if (ctx) {
     char buf[512];
     if (e != cudaSuccess)
@@ -135,20 +40,6 @@ int fail(stq_context *ctx, int status, const char *what, cudaError_t e = cudaSuc
   }
   return status;
 }
-
-#define STQ_CUDA(ctx, call, what)                                        \
-  do {                                                                   \
-    cudaError_t _e = (call);                                             \
-    if (_e != cudaSuccess)                                               \
-      return fail((ctx), _e == cudaErrorMemoryAllocation ? STQ_ERR_NO_MEMORY : STQ_ERR_CUDA, \
-                  (what), _e);                                           \
-  } while (0)
-
-#define STQ_TRY(expr)              \
-  do {                             \
-    const int _st = (expr);        \
-    if (_st != STQ_OK) return _st; \
-  } while (0)
 
 void collect_stage(stq_context *ctx, int st) {
   if (!ctx->pending[st]) return;
@@ -190,16 +81,7 @@ void apply_options(stq_context *ctx) {
 BatchHeader *dev_hdr(stq_context *ctx) {
   return reinterpret_cast<BatchHeader *>(ctx->in_dev.as<char>() + ctx->layout.hdr);
 }
-template <typename T>
-T *dev_at(stq_context *ctx, size_t off) {
-  return reinterpret_cast<T *>(ctx->in_dev.as<char>() + off);
-}
-template <typename T>
-T *host_at(stq_context *ctx, size_t off) {
-  return reinterpret_cast<T *>(ctx->in_host + off);
-}
-
-int read_header(stq_context *ctx, const BatchHeader *src = nullptr) {
+int read_header(stq_context *ctx, const BatchHeader *src) {
   STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_hdr, src ? src : dev_hdr(ctx), sizeof(BatchHeader),
                                 cudaMemcpyDeviceToHost, ctx->stream),
            "read back batch header");
@@ -213,8 +95,6 @@ int read_header(stq_context *ctx, const BatchHeader *src = nullptr) {
     return fail(ctx, STQ_ERR_NO_MEMORY, "cell replicas exceed the replica buffers");
   return STQ_OK;
 }
-
-constexpr int64_t kMaxBoxes = int64_t(INT32_MAX) - 4 * kSortedPad;
 
 int64_t tiles_for(const int64_t *box_off, int S) {
   int64_t t = 0;
@@ -454,7 +334,10 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   return STQ_OK;
 }
 
-}  // namespace
+}  // namespace ctxops
+}  // namespace stq
+
+using namespace stq::ctxops;
 
 extern "C" {
 
@@ -506,6 +389,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
     if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
     if (ctx->graph_event) cudaEventDestroy(ctx->graph_event);
+    if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
                       &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag,
@@ -1012,6 +896,83 @@ int stq_context_stage_times(stq_context *ctx, double *ms, int64_t *calls, int ma
 
 const char *stq_stage_name(int stage) {
   return (stage >= 0 && stage < kStages) ? kStageNames[stage] : "unknown";
+}
+
+int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box_off, int n_scenes,
+                 stq_pair *d_pairs, int64_t capacity, double *best_ms) {
+  if (!ctx || !best_ms || n_scenes < 1 || !h_box_off || capacity < 0 || (capacity > 0 && !d_pairs))
+    return STQ_ERR_INVALID_ARG;
+  DeviceGuard g(ctx->device);
+  *best_ms = 0.0;
+  const int64_t key = (int64_t(bits_for(std::max<int64_t>(h_box_off[n_scenes], 1))) << 32) |
+                      int64_t(bits_for(n_scenes));
+  const int opts[5] = {STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH, STQ_OPT_BLOCK_SIZE,
+                       STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE};
+  for (const auto &kv : ctx->tuned)
+    if (kv.first == key) {
+      for (int o = 0; o < 5; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], kv.second[size_t(o)]));
+      return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO);
+    }
+  const bool was_timing = ctx->timing;
+  ctx->timing = false;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  STQ_CUDA(ctx, cudaEventCreate(&e0), "create event");
+  STQ_CUDA(ctx, cudaEventCreate(&e1), "create event");
+  auto elapsed = [&](const std::function<int()> &fn, float *ms) -> int {
+    float best = 1e30f;
+    for (int rep = 0; rep < 2; ++rep) {
+      STQ_CUDA(ctx, cudaEventRecord(e0, ctx->stream), "record");
+      STQ_TRY(fn());
+      STQ_CUDA(ctx, cudaEventRecord(e1, ctx->stream), "record");
+      STQ_CUDA(ctx, cudaEventSynchronize(e1), "synchronise");
+      float t = 0.f;
+      STQ_CUDA(ctx, cudaEventElapsedTime(&t, e0, e1), "elapsed");
+      best = std::min(best, t);
+    }
+    *ms = best;
+    return STQ_OK;
+  };
+  std::vector<int64_t> best_set(5, 0);
+  float best_total = 1e30f;
+  int st = STQ_OK;
+  for (int64_t scale : {1, 2, 4}) {
+    for (int64_t radix : {8, 4}) {
+      if ((st = stq_context_set_option(ctx, STQ_OPT_CELL_SCALE, scale)) != STQ_OK) break;
+      if ((st = stq_context_set_option(ctx, STQ_OPT_RADIX_BITS, radix)) != STQ_OK) break;
+      float t_prep = 0.f;
+      st = elapsed([&] { return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO); },
+                   &t_prep);
+      if (st != STQ_OK) break;
+      for (int64_t lanes : {4, 8, 16, 32})
+        for (int64_t queue : {32, 64, 128})
+          for (int64_t block : {128, 256, 512}) {
+            stq_context_set_option(ctx, STQ_OPT_LANES_PER_ENTRY, lanes);
+            stq_context_set_option(ctx, STQ_OPT_QUEUE_DEPTH, queue);
+            stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, block);
+            float t_sweep = 0.f;
+            int64_t count = 0, next = 0, total = 0;
+            st = elapsed([&] {
+              const int r = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, &count, &next, &total);
+              return r == STQ_OVERFLOW ? STQ_OK : r;
+            }, &t_sweep);
+            if (st != STQ_OK) break;
+            if (t_prep + t_sweep < best_total) {
+              best_total = t_prep + t_sweep;
+              best_set = {lanes, queue, block, radix, scale};
+            }
+          }
+      if (st != STQ_OK) break;
+    }
+    if (st != STQ_OK) break;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->timing = was_timing;
+  if (st != STQ_OK) return st;
+  for (int o = 0; o < 5; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], best_set[size_t(o)]));
+  ctx->tuned.emplace_back(key, best_set);
+  *best_ms = double(best_total);
+  return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO);
 }
 
 int stq_brute_force(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, stq_pair *d_pairs,

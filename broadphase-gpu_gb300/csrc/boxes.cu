@@ -140,6 +140,26 @@ batch_build_kernel(const double *__restrict__ V0, const double *__restrict__ V1,
   }
 }
 
+// Serving: scene s's mesh lives in its own allocation (MeshRef); the box id
+// is the batch index, vertex ids are local to the scene.
+__global__ void __launch_bounds__(kBuildBlock)
+batch_build_refs_kernel(const MeshRef *__restrict__ refs, const long long *__restrict__ box_off,
+                        BatchHeader *hdr, float r_up, stq_aabb *__restrict__ out) {
+  const int n_scenes = hdr->n_scenes;
+  const int64_t n_boxes = hdr->n_boxes;
+  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_boxes;
+       t += int64_t(gridDim.x) * blockDim.x) {
+    int lo = 0, hi = n_scenes - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (box_off[mid] <= t) lo = mid;
+      else hi = mid - 1;
+    }
+    const MeshRef &m = refs[lo];
+    build_one(m.V0, m.V1, m.nV, m.E, m.nE, m.F, t - box_off[lo], int(t), r_up, out + t, &hdr->flags);
+  }
+}
+
 int grid_for(int64_t n, int block, int cap = 152 * 32) {
   int64_t g = (n + block - 1) / block;
   if (g < 1) g = 1;
@@ -166,6 +186,13 @@ cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V
                                BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out) {
   batch_build_kernel<<<grid_for(box_cap, kBuildBlock), kBuildBlock, 0, s>>>(
       V0, V1, voff, E, eoff, F, foff, box_off, hdr, r_up, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_build_refs(cudaStream_t s, const MeshRef *refs, const long long *box_off,
+                                    BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out) {
+  batch_build_refs_kernel<<<grid_for(box_cap, kBuildBlock), kBuildBlock, 0, s>>>(refs, box_off, hdr,
+                                                                                 r_up, out);
   return cudaGetLastError();
 }
 

@@ -211,6 +211,23 @@ cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V
                                const long long *voff, const int32_t *E, const long long *eoff,
                                const int32_t *F, const long long *foff, const long long *box_off,
                                BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out);
+// A scene held by the serving loop: its own device mesh and time-step state.
+struct MeshRef {
+  double *V0, *V1;
+  const int32_t *E, *F;
+  long long nV, nE, nF;
+  unsigned long long seed;
+  double sigma;
+  int step;   // timestep about to run (0: the submitted positions)
+  int pad;
+};
+cudaError_t launch_advance(cudaStream_t s, const MeshRef *refs, const long long *voff,
+                           const BatchHeader *hdr, int64_t vert_cap);
+cudaError_t launch_batch_build_refs(cudaStream_t s, const MeshRef *refs, const long long *box_off,
+                                    BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out);
+cudaError_t launch_pair_checksums(cudaStream_t s, const stq_pair *pairs, long long capacity,
+                                  const BatchHeader *hdr, const long long *box_off,
+                                  unsigned long long *checks, int scene_cap);
 cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long long *scene_pairs,
                                int scene_cap);
 

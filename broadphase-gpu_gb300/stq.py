@@ -83,6 +83,23 @@ ABI_SIGNATURES = {
     "stq_batch_broadphase": (ctypes.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int,
                                             ctypes.c_float, ctypes.c_int, _vp, ctypes.c_int64, _c_i64p,
                                             _c_i64p, _vp]),
+    "stq_autotune": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int, _vp, ctypes.c_int64,
+                                    ctypes.POINTER(ctypes.c_double)]),
+    "stq_server_create": (ctypes.c_int, [ctypes.c_int, _vp, ctypes.c_int64, ctypes.c_int64, ctypes.c_int,
+                                         ctypes.POINTER(_vp)]),
+    "stq_server_destroy": (None, [_vp]),
+    "stq_server_submit": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp,
+                                         ctypes.c_int64, ctypes.c_int, ctypes.c_double, ctypes.c_uint64,
+                                         _c_i64p]),
+    "stq_server_tick": (ctypes.c_int, [_vp, _vp, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "stq_server_result": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_int)]),
+    "stq_server_mesh": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp]),
+    "stq_server_stats": (ctypes.c_int, [_vp, _c_i64p, _c_i64p, _c_i64p, _c_i64p]),
+    "stq_read_mesh": (ctypes.c_int, [ctypes.c_char_p, _vp, _c_i64p, _vp, _c_i64p]),
+    "stq_mesh_edges": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _c_i64p]),
+    "stq_compare_truth_json": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int64, _c_i64p, _c_i64p,
+                                              _c_i64p]),
     "stq_sweep_static": (ctypes.c_int, [_vp, ctypes.c_int64, ctypes.c_int, _vp, ctypes.c_int64, _c_i64p,
                                         _c_i64p, _vp]),
     "stq_sort_pairs": (ctypes.c_int, [_vp, _vp, ctypes.c_int64]),
@@ -281,6 +298,16 @@ class Context:
         self._check(self.lib.stq_batch_prepare(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1,
                                                None if ax is None else ax.ctypes.data, axis))
 
+    def autotune(self, boxes, box_off, pairs, capacity: int) -> tuple:
+        """Tunes the context's options on this batch; returns (best_ms, settings)."""
+        bo = np.ascontiguousarray(box_off, np.int64)
+        ms = ctypes.c_double()
+        self._check(self.lib.stq_autotune(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1, _ptr(pairs),
+                                          capacity, ctypes.byref(ms)))
+        names = {OPT_LANES: "lanes", OPT_QUEUE: "queue", OPT_BLOCK: "block", OPT_RADIX_BITS: "radix_bits",
+                 OPT_CELL_SCALE: "cell_scale"}
+        return ms.value, {v: self.get_option(k) for k, v in names.items()}
+
     def batch_scene_pairs(self, n_scenes: int) -> np.ndarray:
         out = np.zeros(n_scenes, np.int64)
         self._check(self.lib.stq_batch_scene_pairs(self._h, out.ctypes.data, n_scenes))
@@ -309,6 +336,145 @@ class Context:
         self._check(self.lib.stq_brute_force(self._h, _ptr(boxes), n, _ptr(pairs), capacity,
                                              ctypes.byref(c)), allow=(STQ_OK, STQ_OVERFLOW))
         return c.value
+
+
+class Server:
+    """Continuous-batching serving loop (stq_server*): time-stepped requests,
+    admission by HBM budget, one batched launch per tick."""
+
+    def __init__(self, device: int = 0, stream: int | None = None, budget_bytes: int = 160 << 30,
+                 max_boxes: int = 1 << 24, max_scenes: int = 256):
+        self.lib = load_library()
+        self._h = _vp()
+        st = self.lib.stq_server_create(device, stream, budget_bytes, max_boxes, max_scenes,
+                                        ctypes.byref(self._h))
+        if st != STQ_OK:
+            raise STQError(st, "server creation failed")
+        self.max_scenes = max_scenes
+        self._meshes = {}
+
+    def close(self) -> None:
+        if self._h:
+            self.lib.stq_server_destroy(self._h)
+            self._h = _vp()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def submit(self, mesh: "Mesh", steps: int, sigma: float, seed: int) -> int:
+        rid = ctypes.c_int64()
+        st = self.lib.stq_server_submit(self._h, mesh.V0.ctypes.data, mesh.V1.ctypes.data, mesh.V0.shape[0],
+                                        mesh.E.ctypes.data, mesh.E.shape[0], mesh.F.ctypes.data,
+                                        mesh.F.shape[0], steps, float(sigma), ctypes.c_uint64(seed),
+                                        ctypes.byref(rid))
+        if st != STQ_OK:
+            raise STQError(st, "submit failed")
+        self._meshes[rid.value] = mesh.V0.shape[0]
+        return rid.value
+
+    def tick(self) -> list:
+        ids = (ctypes.c_int64 * 1024)()
+        n = ctypes.c_int()
+        st = self.lib.stq_server_tick(self._h, ids, 1024, ctypes.byref(n))
+        if st != STQ_OK:
+            raise STQError(st, "tick failed")
+        return [ids[i] for i in range(min(n.value, 1024))]
+
+    def result(self, rid: int):
+        counts = np.zeros(4096, np.int64)
+        checks = np.zeros(4096, np.uint64)
+        done = ctypes.c_int()
+        st = self.lib.stq_server_result(self._h, rid, counts.ctypes.data, checks.ctypes.data, 4096,
+                                        ctypes.byref(done))
+        if st != STQ_OK:
+            raise STQError(st, "unknown request")
+        return counts[: done.value].copy(), checks[: done.value].copy()
+
+    def mesh(self, rid: int):
+        nv = self._meshes[rid]
+        V0, V1 = np.empty((nv, 3)), np.empty((nv, 3))
+        st = self.lib.stq_server_mesh(self._h, rid, V0.ctypes.data, V1.ctypes.data)
+        if st != STQ_OK:
+            raise STQError(st, "request not active")
+        return V0, V1
+
+    def stats(self) -> dict:
+        a, q, b, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        self.lib.stq_server_stats(self._h, ctypes.byref(a), ctypes.byref(q), ctypes.byref(b), ctypes.byref(t))
+        return {"active": a.value, "queued": q.value, "bytes": b.value, "ticks": t.value}
+
+
+def read_mesh(path) -> tuple:
+    """(V [nV,3] f64, F [nF,3] i32) of an OBJ or PLY triangle mesh (stq_read_mesh)."""
+    lib = load_library()
+    nv, nf = ctypes.c_int64(), ctypes.c_int64()
+    st = lib.stq_read_mesh(str(path).encode(), None, ctypes.byref(nv), None, ctypes.byref(nf))
+    if st != STQ_OK:
+        raise STQError(st, f"cannot read mesh {path}")
+    V = np.empty((nv.value, 3))
+    F = np.empty((nf.value, 3), np.int32)
+    st = lib.stq_read_mesh(str(path).encode(), V.ctypes.data, ctypes.byref(nv), F.ctypes.data, ctypes.byref(nf))
+    if st != STQ_OK:
+        raise STQError(st, f"cannot read mesh {path}")
+    return V, F
+
+
+def mesh_edges(F: np.ndarray) -> np.ndarray:
+    """Unique undirected edges of triangles F, ordered as libigl's edges()."""
+    lib = load_library()
+    F = np.ascontiguousarray(F, np.int32)
+    ne = ctypes.c_int64()
+    st = lib.stq_mesh_edges(F.ctypes.data, F.shape[0], None, ctypes.byref(ne))
+    if st != STQ_OK:
+        raise STQError(st, "edges")
+    E = np.empty((ne.value, 2), np.int32)
+    st = lib.stq_mesh_edges(F.ctypes.data, F.shape[0], E.ctypes.data, ctypes.byref(ne))
+    if st != STQ_OK:
+        raise STQError(st, "edges")
+    return E
+
+
+def parse_mesh(file_t0, file_t1) -> "Mesh":
+    """parseMesh (src/io.cu:30-51): positions at t0 and t1 from two files with the
+    same faces, edges from the faces."""
+    V0, F0 = read_mesh(file_t0)
+    V1, F1 = read_mesh(file_t1)
+    if V0.shape != V1.shape or not np.array_equal(F0, F1):
+        raise STQError(STQ_ERR_INVALID_INPUT, "t0 and t1 meshes differ in topology")
+    return Mesh(V0, V1, mesh_edges(F1), F1)
+
+
+def compare_truth_json(path, pairs: np.ndarray) -> tuple:
+    """compare_mathematica: (truth pairs found, distinct truth pairs, pairs not in the truth)."""
+    lib = load_library()
+    p = np.ascontiguousarray(pairs, np.int32).reshape(-1, 2)
+    f, t, e = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+    st = lib.stq_compare_truth_json(str(path).encode(), p.ctypes.data, p.shape[0], ctypes.byref(f),
+                                    ctypes.byref(t), ctypes.byref(e))
+    if st != STQ_OK:
+        raise STQError(st, f"cannot read {path}")
+    return f.value, t.value, e.value
+
+
+def pair_checksum(pairs: np.ndarray) -> int:
+    """XOR over pairs of splitmix64((lo << 32) | hi): the serving loop's checksum."""
+    p = np.asarray(pairs, np.int64).reshape(-1, 2)
+    z = (p[:, 0].astype(np.uint64) << np.uint64(32)) | p[:, 1].astype(np.uint64)
+    with np.errstate(over="ignore"):
+        z = z + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return int(np.bitwise_xor.reduce(z)) if len(z) else 0
 
 
 # ---- synthetic scenes (libstq_scenes.so) ----------------------------------------

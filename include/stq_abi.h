@@ -231,6 +231,52 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
  * output order for callers that need one). */
 int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count);
 
+/* ---- autotuning --------------------------------------------------------------
+ * Times prepare + sweep of the given batch (as stq_batch_prepare, all start
+ * boxes) over cell scale {1, 2, 4}, radix digit width {4, 8}, lanes per queue
+ * entry {4, 8, 16, 32} (the work-split width of a start box's run), queue
+ * depth {32, 64, 128} and block size {128, 256, 512}, and keeps the fastest
+ * settings as the context's options. Settings are cached per shape bucket
+ * (log2 of the box count, log2 of the scene count): a later call whose batch
+ * falls in a tuned bucket applies them without timing. *best_ms receives the
+ * prepare + sweep time of the chosen settings (0 on a cache hit). The batch is
+ * left prepared. Replaces the reference's fixed launch setup (src/util.cu:9-56). */
+int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box_off,
+                 int n_scenes, stq_pair *d_pairs, int64_t capacity, double *best_ms);
+
+/* ---- serving: continuous batching of time-stepped requests ------------------
+ * No single counterpart in the reference (its apps run one scene per
+ * process); each tick runs the batched pipeline above over the current
+ * timestep of every admitted request. A request is a mesh (host memory,
+ * copied at submit) run for `steps` timesteps: step 0 sweeps the given
+ * trajectories, every later step first sets t0 <- t1 and t1 <- t1 + N(0,
+ * sigma^2) per coordinate on the device (counter-based generator seeded by
+ * `seed`), so the scene stays in HBM between steps. Requests are admitted
+ * first come, first served while they fit the HBM budget (mesh + estimated
+ * pair buffer), the box capacity of one launch and the scene capacity.
+ * Uploads of newly admitted requests overlap the launch in flight. */
+typedef struct stq_server stq_server;
+
+int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t max_boxes,
+                      int max_scenes, stq_server **out);
+void stq_server_destroy(stq_server *server);
+int stq_server_submit(stq_server *server, const double *h_V0, const double *h_V1, int64_t nV,
+                      const int32_t *h_E, int64_t nE, const int32_t *h_F, int64_t nF, int steps,
+                      double sigma, uint64_t seed, int64_t *request_id);
+/* Collects the launch in flight, retires finished requests (their ids go to
+ * done_ids, up to max_done; *n_done = how many finished), admits queued
+ * requests and launches the next tick without waiting for it. */
+int stq_server_tick(stq_server *server, int64_t *done_ids, int max_done, int *n_done);
+/* Per-timestep results of a request: pair count and the XOR over its pairs
+ * of splitmix64((lo << 32) | hi) with ids local to the request's mesh. */
+int stq_server_result(stq_server *server, int64_t request_id, int64_t *counts,
+                      uint64_t *checksums, int max_steps, int *steps_done);
+/* Current positions of an active request (t0 and t1 of its last step). */
+int stq_server_mesh(stq_server *server, int64_t request_id, double *h_V0, double *h_V1);
+/* active, queued, bytes held for admitted requests, ticks launched */
+int stq_server_stats(stq_server *server, int64_t *active, int64_t *queued, int64_t *bytes,
+                     int64_t *ticks);
+
 /* ---- sweep without any allocation -----------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
  * memory when they need a broad phase: work recorded into a CUDA graph by

@@ -152,3 +152,24 @@ def test_batch_with_empty_and_tiny_scenes(ctx, stq, oracle, cuda):
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
     r = ctx.sweep_prepared(pairs, cap)
     check_batch(oracle, pairs[: r.count].cpu().numpy(), bo, want, ctx.batch_scene_pairs(len(boxes)))
+
+
+def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes):
+    import torch
+
+    meshes, want = scenes
+    V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
+    n = sum(m.num_boxes for m in meshes)
+    boxes = torch.empty((n, 11), dtype=torch.int32, device=cuda)
+    bo = ctx.batch_build_boxes(dev(V0, cuda), dev(V1, cuda), vo, dev(E, cuda), eo, dev(F, cuda), fo, boxes)
+    cap = sum(len(w) for w in want) + 16
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    ms, settings = ctx.autotune(boxes, bo, pairs, cap)
+    assert ms > 0
+    assert settings["lanes"] in (4, 8, 16, 32) and settings["queue"] in (32, 64, 128)
+    assert settings["block"] in (128, 256, 512) and settings["radix_bits"] in (4, 8)
+    assert settings["cell_scale"] in (1, 2, 4)
+    r = ctx.sweep_prepared(pairs, cap)
+    check_batch(oracle, pairs[: r.count].cpu().numpy(), bo, want, ctx.batch_scene_pairs(len(meshes)))
+    ms2, settings2 = ctx.autotune(boxes, bo, pairs, cap)  # same shape bucket: cached
+    assert ms2 == 0 and settings2 == settings
