@@ -279,6 +279,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the autotuner (use the library defaults), e.g. for profiling")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rate", type=float, default=100.0)
     args = ap.parse_args()
@@ -331,7 +333,9 @@ def main():
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
     # the project's autotuner picks cell scale, radix width, lane-group width,
     # queue depth and block size for this workload (not timed)
-    tune_ms, tuned = ctx.autotune(boxes, [0, n], pairs, cap)
+    tuned = "library defaults"
+    if not args.no_tune:
+        tune_ms, tuned = ctx.autotune(boxes, [0, n], pairs, cap)
 
     def step():
         ctx.build_boxes(V0, V1, E, F, boxes)

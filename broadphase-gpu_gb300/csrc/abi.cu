@@ -191,6 +191,9 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
   b.offsets = ctx->offsets.as<uint32_t>();
   b.keys = ctx->keys64[0].as<unsigned long long>();
   b.vals = ctx->vals[0].as<uint32_t>();
+  b.seg_count = ctx->seg_count.as<uint32_t>();
+  b.seg_scan = ctx->seg_scan.as<uint32_t>();
+  b.seg_cap = ctx->seg_cap;
   b.box_cap = ctx->box_cap;
   b.rep_cap = ctx->rep_cap;
   b.scene_cap = ctx->scene_cap;
@@ -215,11 +218,18 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
   STQ_CUDA(ctx, ctx->sort_ws.ensure(std::max(radix_workspace_bytes(int64_t(r), 8, 8),
                                               radix_workspace_bytes(int64_t(r), 8, 4))),
            "allocate sort workspace");
-  const size_t slots = r + size_t(cells_cap) + 1 + kSortedPad;
+  // three lists (vertices, edges, faces) per cell, each followed by a sentinel
+  const int64_t segs = std::max<int64_t>(3 * cells_cap, ctx->seg_cap);
+  STQ_CUDA(ctx, ctx->seg_count.ensure(sizeof(uint32_t) * size_t(segs)), "allocate segment counts");
+  STQ_CUDA(ctx, ctx->seg_scan.ensure(sizeof(uint32_t) * size_t(segs + 1)), "allocate segment offsets");
+  STQ_CUDA(ctx, ctx->seg_scan_ws.ensure(scan_workspace_bytes(segs) + 16), "allocate segment scan");
+  ctx->seg_cap = segs;
+  const size_t slots = r + size_t(segs) + 1 + kSortedPad;
   STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->partner.ensure(sizeof(int) * slots), "allocate sorted scene");
   ctx->rep_cap = int64_t(r);
   ctx->slot_cap = int64_t(slots);
   return STQ_OK;
@@ -247,8 +257,15 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b) {
 }
 
 // Keys, sort, sentinels and gather.
-int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int cell_bits) {
+int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits) {
+  STQ_CUDA(ctx, cudaMemsetAsync(b.seg_count, 0, sizeof(uint32_t) * size_t(b.seg_cap), ctx->stream),
+           "clear segment counts");
   STQ_CUDA(ctx, launch_batch_emit(ctx->stream, b), "launch replica emit");
+  uint32_t *seg_total = reinterpret_cast<uint32_t *>(ctx->seg_scan_ws.as<char>() +
+                                                     scan_workspace_bytes(b.seg_cap));
+  STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.seg_count, b.seg_scan, b.seg_cap,
+                                   ctx->seg_scan_ws.ptr, seg_total, &ctx->launches),
+           "launch segment scan");
   stage_end(ctx, kKeys);
   unsigned long long *kb[2] = {ctx->keys64[0].as<unsigned long long>(),
                                ctx->keys64[1].as<unsigned long long>()};
@@ -256,7 +273,7 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int cell_bits)
   int which = 0;
   stage_begin(ctx, kSort);
   const int rbits = ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
-  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, ctx->rep_cap, 0, 32 + cell_bits,
+  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, ctx->rep_cap, 0, 32 + seg_bits,
                                     ctx->sort_ws.ptr, &which, &ctx->launches, &b.hdr->replicas,
                                     rbits),
            "launch radix sort");
@@ -265,14 +282,15 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int cell_bits)
   ctx->scene.syz = ctx->syz.as<float4>();
   ctx->scene.sv = ctx->sv.as<int4>();
   ctx->scene.sflag = ctx->sflag.as<int>();
+  ctx->scene.partner = ctx->partner.as<int>();
   stage_begin(ctx, kGather);
   STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, b.hdr, ctx->slot_cap),
            "launch sentinel fill");
   STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, ctx->rep_cap,
-                                    b.cell_base, b.scenes, ctx->scene),
+                                    b.cell_base, b.scenes, b.seg_count, b.seg_scan, ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
-  ctx->launches += 3;
+  ctx->launches += 4;
   return STQ_OK;
 }
 
@@ -291,14 +309,14 @@ int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_
   STQ_TRY(enqueue_prepare_front(ctx, b));
   STQ_TRY(read_header(ctx));
   const int64_t R = ctx->h_hdr->replicas, cells = ctx->h_hdr->cells;
-  if (R + cells + 1 + kSortedPad > int64_t(INT32_MAX))
+  if (R + 3 * cells + 1 + kSortedPad > int64_t(INT32_MAX))
     return fail(ctx, STQ_ERR_NO_MEMORY, "too many cell replicas for 32-bit positions");
   STQ_TRY(ensure_replica_buffers(ctx, std::max(R, ctx->rep_cap), cells));
   b = batch_buffers(ctx, d_boxes);
-  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(cells)));
+  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * cells)));
   ctx->n_scenes = S;
   ctx->n_boxes = N;
-  ctx->length = R + cells - 1;
+  ctx->length = R > 0 ? R + 3 * cells - 1 : 0;
   ctx->scene.length = ctx->length;
   ctx->prepared = true;
   return STQ_OK;
@@ -324,8 +342,10 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.work = &hdr->work;
   p.box_counts = ctx->box_counts.as<int32_t>();
   p.sflag = ctx->scene.sflag;
+  p.partner = ctx->scene.partner;
   p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
   p.hdr = hdr;
+  p.stats = &hdr->candidates;
   STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
   stage_begin(ctx, count_mode ? kCountSweep : kSweep);
   STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
@@ -392,7 +412,8 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
-                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag,
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->partner,
+                      &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws,
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
                       &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux})
       b->release();
@@ -469,6 +490,10 @@ const char *stq_context_last_error(const stq_context *ctx) {
 }
 
 int64_t stq_context_launch_count(const stq_context *ctx) { return ctx ? ctx->launches : -1; }
+
+int64_t stq_context_candidates(const stq_context *ctx) {
+  return ctx ? int64_t(ctx->h_hdr->candidates) : -1;
+}
 
 int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
                     const int32_t *d_E, int64_t nE, const int32_t *d_F, int64_t nF,
@@ -676,7 +701,7 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
            "allocate batch boxes");
   fill_staging(ctx, box_off.data(), n_scenes, nullptr, axis, h_vert_off, h_edge_off, h_face_off);
   const stq_aabb *boxes = ctx->batch_boxes.as<stq_aabb>();
-  const int cell_bits = bits_for(cells_cap);
+  const int cell_bits = bits_for(3 * cells_cap);
   auto enqueue_all = [&]() -> int {
     STQ_TRY(upload_staging(ctx));
     stage_begin(ctx, kBuild);

@@ -359,18 +359,20 @@ batch_count_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
     counts[i] = 0u;
 }
 
-// ---- 6. replica keys: (global cell id << 32) | order-preserving min --------------
+// ---- 6. replica keys: (segment << 32) | order-preserving min, where the
+// segment is (global cell, box type): every cell holds a vertex, an edge and
+// a face list. Also counts replicas per segment.
 __global__ void __launch_bounds__(kBlock)
 batch_emit_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
                   const SceneRecord *__restrict__ scenes, const unsigned int *__restrict__ cell_base,
                   BatchHeader *hdr, const uint32_t *__restrict__ offsets,
                   unsigned long long *__restrict__ keys, uint32_t *__restrict__ vals,
-                  long long rep_cap) {
-  const bool fits = (long long)hdr->replicas <= rep_cap;
+                  uint32_t *__restrict__ seg_count, long long rep_cap, long long seg_cap) {
+  const bool fits = (long long)hdr->replicas <= rep_cap && 3ll * hdr->cells <= seg_cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    // on overflow of the replica buffers nothing is emitted or swept
-    // every cell is followed by its sentinel; the last one is not a start position
-    hdr->length = fits && hdr->cells > 0 ? hdr->replicas + hdr->cells - 1 : 0u;
+    // each of the 3 lists of a cell is followed by its sentinel; the last
+    // sentinel is not a start position. On overflow nothing is emitted.
+    hdr->length = fits && hdr->cells > 0 && hdr->replicas > 0 ? hdr->replicas + 3 * hdr->cells - 1 : 0u;
     if (!fits) {
       atomicOr(&hdr->flags, kFlagReplicaOverflow);
       hdr->replicas = 0;
@@ -385,11 +387,14 @@ batch_emit_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict_
     const stq_aabb &x = boxes[bi];
     const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
     const unsigned long long xk = float_key(x.min[g.axis]);
+    const unsigned long long type = type_of(x.vertex_ids[1], x.vertex_ids[2]);
     uint32_t o = offsets[bi];
     for (int cb = q.b0; cb <= q.b1; ++cb)
       for (int cc = q.c0; cc <= q.c1; ++cc) {
-        keys[o] = ((cb0 + (unsigned long long)(cb * g.nc + cc)) << 32) | xk;
+        const unsigned long long seg = (cb0 + (unsigned long long)(cb * g.nc + cc)) * 3ull + type;
+        keys[o] = (seg << 32) | xk;
         vals[o] = uint32_t(bi);
+        atomicAdd(&seg_count[seg], 1u);
         ++o;
       }
   }
@@ -404,25 +409,36 @@ fill_sentinels_kernel(float2 *__restrict__ sx, const BatchHeader *hdr, int64_t s
     sx[k] = make_float2(q, q);
 }
 
-// Sorted replica p of global cell c goes to position p + c: every cell is
-// followed by one NaN slot, which ends every x-run at the cell boundary.
+// Sorted replica p of segment s (cell c, type t; s = 3c + t) goes to
+// position p + s: every list is followed by one NaN slot, which ends every
+// run at its list (and cell, and scene) boundary.
 // sflag of a position: bit 0 set if the cell is the box's first cell along b,
 // bit 1 if it is its first cell along c, scene index above. Since the cell
 // coordinate is monotone, the cell of a pair's reference point (max of the
 // two minima on b, on c) is the max of the two boxes' first cells; both boxes
 // lie in this cell, so the reference point is here exactly when, on each of
 // b and c, one of the two replicas is its box's first cell.
+// partner of a position: its first candidate. An edge's candidates are the
+// edges after it in its list; a vertex's are the cell's faces whose min is
+// >= its min (lower bound), a face's the cell's vertices whose min is > its
+// min (upper bound): every V-F pair that overlaps on the sweep axis is found
+// once, from the box with the smaller min (the vertex on ties), and vertex-
+// vertex, edge-face and face-face candidates are never tested.
 __global__ void __launch_bounds__(kBlock)
 gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long *__restrict__ keys,
                     const uint32_t *__restrict__ order, const BatchHeader *hdr,
                     const unsigned int *__restrict__ cell_base,
-                    const SceneRecord *__restrict__ scenes, float2 *__restrict__ sx,
-                    float4 *__restrict__ syz, int4 *__restrict__ sv, int *__restrict__ sflag) {
+                    const SceneRecord *__restrict__ scenes, const uint32_t *__restrict__ seg_count,
+                    const uint32_t *__restrict__ seg_scan, float2 *__restrict__ sx,
+                    float4 *__restrict__ syz, int4 *__restrict__ sv, int *__restrict__ sflag,
+                    int *__restrict__ partner) {
   const int64_t R = hdr->replicas;
   const int S = hdr->n_scenes;
   for (int64_t p = blockIdx.x * int64_t(kBlock) + threadIdx.x; p < R;
        p += int64_t(gridDim.x) * kBlock) {
-    const unsigned int cell = unsigned(keys[p] >> 32);
+    const unsigned long long key = keys[p];
+    const unsigned int seg = unsigned(key >> 32);
+    const unsigned int cell = seg / 3u, type = seg - 3u * cell;
     const uint32_t bi = order[p];
     int lo = 0, hi = S - 1;  // scene of the cell
     while (lo < hi) {
@@ -438,11 +454,26 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
     const int cb = local / g.nc, cc = local - cb * g.nc;
     const int fb = cell_coord(x.min[b], g.ob, g.ib, g.nb) == cb;
     const int fc = cell_coord(x.min[c], g.oc, g.ic, g.nc) == cc;
-    const int64_t k = p + cell;
+    const int64_t k = p + seg;
+    int64_t first = k + 1;
+    if (type != 1u) {
+      // bound search of this min among the other list's sorted keys
+      const unsigned int other = 3u * cell + (type == 0u ? 2u : 0u);
+      const uint32_t xk = uint32_t(key & 0xffffffffu);
+      uint32_t a = seg_scan[other], e = a + seg_count[other];
+      while (a < e) {
+        const uint32_t mid = (a + e) >> 1;
+        const uint32_t mk = uint32_t(keys[mid] & 0xffffffffu);
+        if (type == 0u ? mk < xk : mk <= xk) a = mid + 1;
+        else e = mid;
+      }
+      first = int64_t(a) + other;
+    }
     sx[k] = make_float2(x.min[g.axis], x.max[g.axis]);
     syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
     sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
     sflag[k] = (lo << 2) | (fc << 1) | fb;
+    partner[k] = int(first);
   }
 }
 
@@ -459,6 +490,7 @@ reset_sweep_kernel(BatchHeader *hdr, unsigned long long *scene_pairs) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     hdr->pairs = 0ull;
     hdr->work = 0;
+    hdr->candidates = 0ull;
   }
 }
 
@@ -493,7 +525,7 @@ cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b) {
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b) {
   batch_emit_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.cell_base,
                                                             b.hdr, b.offsets, b.keys, b.vals,
-                                                            b.rep_cap);
+                                                            b.seg_count, b.rep_cap, b.seg_cap);
   return cudaGetLastError();
 }
 
@@ -507,10 +539,12 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
+                                const uint32_t *seg_count, const uint32_t *seg_scan,
                                 SortedScene scene) {
   gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
-                                                             scenes, scene.sx, scene.syz, scene.sv,
-                                                             scene.sflag);
+                                                             scenes, seg_count, seg_scan, scene.sx,
+                                                             scene.syz, scene.sv, scene.sflag,
+                                                             scene.partner);
   return cudaGetLastError();
 }
 

@@ -74,7 +74,9 @@ struct stq_context {
   char *in_host = nullptr;
   size_t in_host_bytes = 0;
   DevBuf scenes, cell_base, scene_pairs, counts, offsets, scan_ws, keys64[2], vals[2], sort_ws;
-  DevBuf sx, syz, sv, sflag, box_counts, prefix_ws, pair_keys[2];
+  DevBuf sx, syz, sv, sflag, partner, box_counts, prefix_ws, pair_keys[2];
+  DevBuf seg_count, seg_scan, seg_scan_ws;  // replicas per (cell, type) list
+  int64_t seg_cap = 0;
   DevBuf batch_boxes, e2e_boxes, e2e_pairs, e2e_mesh;
   DevBuf aux;  // header of calls outside a batch (box build, all-pairs check)
 
@@ -133,7 +135,8 @@ int ensure_box_buffers(stq_context *ctx, int64_t box_cap);
 int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap);
 int bits_for(int64_t v);
 int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b);
-int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int cell_bits);
+// seg_bits: bits of the largest segment id (3 x cells)
+int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits);
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs, long long capacity,
               bool count_mode);
 

@@ -205,7 +205,7 @@ int enqueue_tick(stq_server *sv, bool advance) {
            "launch box build");
   const BatchBuffers b = batch_buffers(ctx, ctx->batch_boxes.as<stq_aabb>());
   STQ_TRY(enqueue_prepare_front(ctx, b));
-  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(sv->max_boxes / 16 + sv->max_scenes + 1)));
+  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * (sv->max_boxes / 16 + sv->max_scenes + 1))));
   STQ_TRY(run_sweep(ctx, 0, ctx->slot_cap, sv->pairs.as<stq_pair>(), sv->pair_cap, false));
   STQ_CUDA(ctx, launch_pair_checksums(ctx->stream, sv->pairs.as<stq_pair>(), sv->pair_cap, hdr, box_off,
                                       sv->checks_dev.as<unsigned long long>(), sv->max_scenes),
@@ -377,7 +377,8 @@ int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t ma
   cudaMemGetInfo(&free_b, &total);
   sv->fixed = int64_t(ctx->in_dev.bytes + ctx->counts.bytes + ctx->offsets.bytes + ctx->scan_ws.bytes +
                       ctx->keys64[0].bytes * 2 + ctx->vals[0].bytes * 2 + ctx->sort_ws.bytes + ctx->sx.bytes +
-                      ctx->syz.bytes + ctx->sv.bytes + ctx->sflag.bytes + ctx->batch_boxes.bytes);
+                      ctx->syz.bytes + ctx->sv.bytes + ctx->sflag.bytes + ctx->partner.bytes +
+                      ctx->seg_count.bytes + ctx->seg_scan.bytes + ctx->batch_boxes.bytes);
   if (sv->fixed >= budget_bytes) return bad(STQ_ERR_NO_MEMORY);
   *out = sv.release();
   return STQ_OK;

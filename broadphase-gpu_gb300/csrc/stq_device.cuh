@@ -57,11 +57,19 @@ __host__ __device__ inline float ref_next_down(float x) {
 }
 
 // ---- order-preserving float -> uint32 key -----------------------------------
-// Radix order refines float '<': -0 sorts just before +0 (they compare equal,
-// so the sweep treats either order alike); NaN is rejected before sorting.
+// Key order is float '<' order with -0 and +0 equal (both map to the key of
+// +0), so key equality is float equality and bound searches on keys agree
+// with the float tests of the sweep; NaN is rejected before sorting.
 __device__ __forceinline__ uint32_t float_key(float f) {
   uint32_t b = __float_as_uint(f);
+  if (b == 0x80000000u) b = 0u;
   return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+
+// Box type from the signs of vertexIds (src/aabb.cu:12-31): vertex 0, edge
+// 1, face 2.
+__device__ __forceinline__ int type_of(int v1, int v2) {
+  return v2 >= 0 ? 2 : (v1 >= 0 ? 1 : 0);
 }
 
 // Cell coordinate of a bound: clamp(floor((v - origin) * inv), 0, n - 1),

@@ -105,7 +105,7 @@ struct BatchHeader {
   int flags;                // kFlag* bits
   unsigned int replicas;    // R, cell replicas
   unsigned int cells;       // total cells of all scenes
-  unsigned int length;      // sweep positions: R + cells
+  unsigned int length;      // sweep positions: R + 3 * cells - 1
   int work;                 // sweep grab cursor
   unsigned long long pairs; // pairs found by the last sweep
   long long prefix;         // overflow: start positions of the prefix that fits
@@ -113,6 +113,7 @@ struct BatchHeader {
   int budget;               // replica budget: replicas <= budget * boxes per scene
   int n_tiles;              // input: entries of the tile table
   int pad;
+  unsigned long long candidates;  // candidates tested by the last sweep
 };
 
 // A tile of at most kTileBoxes consecutive boxes of one scene (built by the
@@ -139,6 +140,7 @@ struct SortedScene {
   float4 *syz = nullptr;  // (min_b, min_c, max_b, max_c) on the other axes
   int4 *sv = nullptr;     // (vertexIds[0..2], id)
   int *sflag = nullptr;   // first-cell bits (0: along b, 1: along c), scene << 2
+  int *partner = nullptr; // first candidate position of each start position
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
 
@@ -154,8 +156,10 @@ struct SweepParams {
   int *work;
   int32_t *box_counts;       // count mode: pairs per start position (k - begin)
   const int *sflag;          // first-cell bits and scene of each position
+  const int *partner;        // first candidate position of each start position
   unsigned long long *scene_pairs;  // per-scene pair counters
   const BatchHeader *hdr;    // device sizes (length bounds the sweep range)
+  unsigned long long *stats; // candidates tested (may be null)
 };
 
 // ---- launch wrappers (each returns the launch error) -------------------------
@@ -190,6 +194,9 @@ struct BatchBuffers {
   uint32_t *counts, *offsets;   // per box
   unsigned long long *keys;     // replica keys (sort input)
   uint32_t *vals;               // replica box indices (sort input)
+  uint32_t *seg_count;          // replicas per segment (cell x type), seg_cap entries
+  uint32_t *seg_scan;           // exclusive scan of seg_count
+  long long seg_cap;
   long long box_cap;            // capacities
   long long rep_cap;
   int scene_cap;
@@ -204,6 +211,7 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
+                                const uint32_t *seg_count, const uint32_t *seg_scan,
                                 SortedScene scene);
 // Batched box build: scene s has vertices [voff[s], voff[s+1]) etc.; box ids
 // are global (box_off[s] + local), vertex ids local to the scene.

@@ -9,8 +9,10 @@
 // GB300 design. Each warp owns a shared-memory ring of pending start boxes
 // (the "tiniest queue"). The warp is split into lane groups of G lanes; a
 // group takes one start box k from the ring and walks its x-run
-// j = k+1, k+2, ... G candidates per step, until the first j whose min
-// exceeds k's max (a NaN sentinel ends every run). A group that finishes
+// j = partner[k], partner[k]+1, ... G candidates per step, until the first j
+// whose min exceeds k's max (a NaN sentinel ends every run). partner[k] is
+// k+1 for an edge, and the first face (for a vertex) or vertex (for a face)
+// of the same cell's list at or after k's min. A group that finishes
 // takes the next pending box, so a long run never stalls the other groups.
 // Refill, hand-out and pair output use __ballot_sync/__popc compaction: no
 // shared-memory atomics, and one global atomic per warp step that emits.
@@ -63,6 +65,7 @@ stq_sweep_kernel(const SweepParams p) {
   const int end = min(p.end, int(p.hdr->length));
   const int span = end - p.begin;
   int kf = 0;  // first-cell bits and scene of the current start box
+  unsigned tested = 0;  // candidates this lane tested (statistics)
   // warp-uniform: staged pairs, and pairs of the current scene not yet added
   // to its counter
   int staged = 0;
@@ -87,7 +90,7 @@ stq_sweep_kernel(const SweepParams p) {
       const int take = min(32, min(Q - qsize, chunk_end - next_k));
       const int kk = next_k + lane;
       bool push = false;
-      if (lane < take) push = p.sx[kk + 1].x <= p.sx[kk].y;
+      if (lane < take) push = p.sx[p.partner[kk]].x <= p.sx[kk].y;
       const unsigned m = __ballot_sync(kFullMask, push);
       if (push) q[(qhead + qsize + __popc(m & lanemask_lt())) & (Q - 1)] = kk;
       qsize += __popc(m);
@@ -102,7 +105,7 @@ stq_sweep_kernel(const SweepParams p) {
       const int r = __popc(needm & leaders_below);
       if (r < ntake) {
         k = q[(qhead + r) & (Q - 1)];
-        j0 = k + 1;
+        j0 = p.partner[k];
         kmax = p.sx[k].y;
         kb = p.syz[k];
         kv = p.sv[k];
@@ -127,15 +130,18 @@ stq_sweep_kernel(const SweepParams p) {
     bool hit = false;
     int lo_id = 0, hi_id = 0;
     if (valid) {
+      ++tested;
       const float4 b = p.syz[j];
-      const int4 bv = p.sv[j];
-      hit = overlap_bc(kb, b) && valid_pair(kv, bv) && !covertex(kv, bv);
+      if (overlap_bc(kb, b)) {  // ids only for candidates that overlap on b and c
+        const int4 bv = p.sv[j];
+        hit = valid_pair(kv, bv) && !covertex(kv, bv);
       // a pair found in several cells is emitted only in the cell of its
       // reference point: on b and on c, one of the two replicas must be its
       // box's first cell (the candidate's bits are read only when needed)
-      if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j]) & 3) == 3;
-      lo_id = min(kv.w, bv.w);
-      hi_id = max(kv.w, bv.w);
+        if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j]) & 3) == 3;
+        lo_id = min(kv.w, bv.w);
+        hi_id = max(kv.w, bv.w);
+      }
     }
     // 4. Emit: compact the step's hits into the warp's staging buffer; append
     //    it to the pair list with one global atomic per 32 or more pairs.
@@ -179,6 +185,8 @@ stq_sweep_kernel(const SweepParams p) {
     __syncwarp();
     if (staged) flush_staged(st, staged, lane, p);
     if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+    const unsigned t = __reduce_add_sync(kFullMask, tested);
+    if (lane == 0 && p.stats) atomicAdd(p.stats, (unsigned long long)t);
   }
 }
 

@@ -58,6 +58,7 @@ ABI_SIGNATURES = {
     "stq_context_get_option": (ctypes.c_int64, [_vp, ctypes.c_int]),
     "stq_context_last_error": (ctypes.c_char_p, [_vp]),
     "stq_context_launch_count": (ctypes.c_int64, [_vp]),
+    "stq_context_candidates": (ctypes.c_int64, [_vp]),
     "stq_build_boxes": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64,
                                        _vp, ctypes.c_int64, ctypes.c_float, _vp]),
     "stq_select_axis": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
@@ -203,6 +204,11 @@ class Context:
 
     def get_option(self, option: int) -> int:
         return int(self.lib.stq_context_get_option(self._h, option))
+
+    @property
+    def candidates(self) -> int:
+        """Candidates the last sweep tested."""
+        return int(self.lib.stq_context_candidates(self._h))
 
     @property
     def launches(self) -> int:

@@ -111,6 +111,9 @@ int64_t stq_context_get_option(const stq_context *ctx, int option);
 const char *stq_context_last_error(const stq_context *ctx);
 /* Kernel launches this context issued since it was created. */
 int64_t stq_context_launch_count(const stq_context *ctx);
+/* Candidates (x-overlapping start box / candidate pairs) the last sweep
+ * tested, a measure of the sweep's work beyond the pairs it found. */
+int64_t stq_context_candidates(const stq_context *ctx);
 
 /* Swept boxes from vertex trajectories. d_V0/d_V1 are row-major [nV x 3]
  * fp64 positions at t0 and t1, d_E [nE x 2] and d_F [nF x 3] int32 vertex
@@ -133,10 +136,11 @@ int stq_prepare(stq_context *ctx, const stq_aabb *d_boxes, int64_t n,
                 int axis);
 
 /* Number of sweep positions of the prepared scene: the start-box cursor of
- * stq_sweep_prepared runs over [0, length). Equal to the box count when
- * cells are off; with cells, boxes are replicated into the cells they touch
- * and every cell but the last is followed by one empty position. -1 if
- * nothing is prepared. */
+ * stq_sweep_prepared runs over [0, length). Boxes are replicated into the
+ * cells they touch (one cell when STQ_OPT_CELLS = 1); every cell holds a
+ * vertex, an edge and a face list, each followed by one empty position, so
+ * length = replicas + 3 * cells - 1 (n + 2 with one cell; 0 with no boxes).
+ * -1 if nothing is prepared. */
 int64_t stq_prepared_length(const stq_context *ctx);
 
 /* Sweeps start boxes [start, start + max_start) of the prepared scene in

@@ -18,8 +18,8 @@
 // MAX_OVERLAP_CUTOFF and sweeps again; tidstart is the resume cursor.
 // Differences: pairs are (smaller id, larger id); errors throw
 // stq::gpu::Error instead of calling exit(); tidstart counts positions of the
-// prepared sweep order (stq_prepared_length), which equal box indices when
-// cells are off (STQ_OPT_CELLS = 1); devcount is ignored (one GPU).
+// prepared sweep order (stq_prepared_length: replicas of boxes in cells, in
+// vertex, edge and face lists); devcount is ignored (one GPU).
 #pragma once
 
 #include <cuda_runtime.h>

@@ -205,8 +205,8 @@ def test_max_start_batches(ctx, stq, oracle, cuda, c0):
         ctx.set_option(stq.OPT_CELLS, cells)
         ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
         length = ctx.prepared_length
-        if cells == 1:
-            assert length == len(boxes)
+        if cells == 1:  # one cell: vertex, edge and face lists, two inner sentinels
+            assert length == len(boxes) + 2
         start, parts = 0, []
         while start < length:
             r = ctx.sweep_prepared(pairs, cap, start=start, max_start=length // 5 + 1)
@@ -240,7 +240,7 @@ def test_empty_and_tiny(ctx, stq, oracle, cuda):
     one = np.zeros(1, stq.AABB_DTYPE)
     one[0] = (0, [0, 0, 0], [1, 1, 1], [0, -1, -1], 0)
     r = ctx.sweep(boxes_dev(one, cuda), 1, pairs, 4)
-    assert (r.status, r.count, r.next_start) == (stq.STQ_OK, 0, 1)
+    assert (r.status, r.count, r.next_start) == (stq.STQ_OK, 0, ctx.prepared_length)
     r = ctx.sweep(boxes_dev(one, cuda), 1, pairs, 0)
     assert r.count == 0
 
@@ -337,7 +337,7 @@ def test_cells_fixed_grids(ctx, stq, oracle, cuda, c0, cells):
         got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
         assert np.array_equal(got, want), (cells, axis)
         if cells == 1:
-            assert ctx.prepared_length == len(boxes)
+            assert ctx.prepared_length == len(boxes) + 2
 
 
 @pytest.mark.parametrize("scale", [1, 2, 4, 16])
