@@ -141,6 +141,7 @@ void fill_staging(stq_context *ctx, const int64_t *box_off, int S, const int *ax
   BatchHeader *h = host_at<BatchHeader>(ctx, L.hdr);
   std::memset(h, 0, sizeof(BatchHeader));
   h->n_boxes = box_off[S];
+  h->box_count = uint32_t(box_off[S]);
   h->n_scenes = S;
   h->budget = ctx->budget;
   long long *bo = host_at<long long>(ctx, L.box_off);
@@ -191,6 +192,11 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
   b.offsets = ctx->offsets.as<uint32_t>();
   b.keys = ctx->keys64[0].as<unsigned long long>();
   b.vals = ctx->vals[0].as<uint32_t>();
+  b.box_keys = ctx->bkeys[0].as<uint32_t>();
+  b.box_vals = ctx->bvals[0].as<uint32_t>();
+  b.box_keys2 = ctx->bkeys[1].as<uint32_t>();
+  b.box_vals2 = ctx->bvals[1].as<uint32_t>();
+  b.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
   b.seg_count = ctx->seg_count.as<uint32_t>();
   b.seg_scan = ctx->seg_scan.as<uint32_t>();
   b.seg_cap = ctx->seg_cap;
@@ -205,6 +211,13 @@ int ensure_box_buffers(stq_context *ctx, int64_t box_cap) {
   STQ_CUDA(ctx, ctx->counts.ensure(sizeof(uint32_t) * n), "allocate replica counts");
   STQ_CUDA(ctx, ctx->offsets.ensure(sizeof(uint32_t) * n), "allocate replica offsets");
   STQ_CUDA(ctx, ctx->scan_ws.ensure(scan_workspace_bytes(int64_t(n))), "allocate scan workspace");
+  for (int b = 0; b < 2; ++b) {
+    STQ_CUDA(ctx, ctx->bkeys[b].ensure(sizeof(uint32_t) * n), "allocate box keys");
+    STQ_CUDA(ctx, ctx->bvals[b].ensure(sizeof(uint32_t) * n), "allocate box order");
+  }
+  STQ_CUDA(ctx, ctx->sort_ws.ensure(std::max(radix_workspace_bytes(int64_t(n), 4, 8),
+                                              radix_workspace_bytes(int64_t(n), 4, 4))),
+           "allocate sort workspace");
   ctx->box_cap = int64_t(n);
   return STQ_OK;
 }
@@ -241,42 +254,59 @@ int bits_for(int64_t v) {
   return b;
 }
 
-// Statistics, axis, grid and replica counts: everything before the sort.
-int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b) {
+int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_boxes) {
   stage_begin(ctx, kAxis);
   STQ_CUDA(ctx, launch_batch_stats(ctx->stream, b), "launch batch statistics");
   STQ_CUDA(ctx, launch_batch_policy(ctx->stream, b), "launch batch policy");
   stage_end(ctx, kAxis);
+  // boxes in sweep-axis order: the emit then writes every list in key order
+  stage_begin(ctx, kSort);
+  STQ_CUDA(ctx, launch_batch_box_keys(ctx->stream, b), "launch box keys");
+  uint32_t *kb[2] = {ctx->bkeys[0].as<uint32_t>(), ctx->bkeys[1].as<uint32_t>()};
+  uint32_t *vb[2] = {ctx->bvals[0].as<uint32_t>(), ctx->bvals[1].as<uint32_t>()};
+  const int rbits = ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
+  const int64_t n = n_boxes >= 0 ? n_boxes : ctx->box_cap;
+  STQ_CUDA(ctx, radix_sort_u32(ctx->stream, kb, vb, n, rbits, ctx->sort_ws.ptr, &ctx->order_buf, &ctx->launches,
+                               n_boxes >= 0 ? nullptr : &b.hdr->box_count),
+           "launch box sort");
+  stage_end(ctx, kSort);
+  BatchBuffers bs = b;
+  bs.order = vb[ctx->order_buf];
   stage_begin(ctx, kKeys);
-  STQ_CUDA(ctx, launch_batch_counts(ctx->stream, b), "launch replica counts");
+  STQ_CUDA(ctx, launch_batch_counts(ctx->stream, bs, n), "launch replica counts");
   STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.counts, b.offsets, ctx->box_cap, ctx->scan_ws.ptr,
                                    &b.hdr->replicas, &ctx->launches),
            "launch replica scan");
-  ctx->launches += 5;
+  ctx->launches += 6;
   return STQ_OK;
 }
 
-// Keys, sort, sentinels and gather.
-int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits) {
+int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, int64_t n_boxes,
+                         int64_t replicas) {
   STQ_CUDA(ctx, cudaMemsetAsync(b.seg_count, 0, sizeof(uint32_t) * size_t(b.seg_cap), ctx->stream),
            "clear segment counts");
-  STQ_CUDA(ctx, launch_batch_emit(ctx->stream, b), "launch replica emit");
+  BatchBuffers bs = b;
+  bs.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
+  STQ_CUDA(ctx, launch_batch_emit(ctx->stream, bs, n_boxes >= 0 ? n_boxes : ctx->box_cap, ctx->num_sms),
+           "launch replica emit");
   uint32_t *seg_total = reinterpret_cast<uint32_t *>(ctx->seg_scan_ws.as<char>() +
                                                      scan_workspace_bytes(b.seg_cap));
   STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.seg_count, b.seg_scan, b.seg_cap,
                                    ctx->seg_scan_ws.ptr, seg_total, &ctx->launches),
            "launch segment scan");
   stage_end(ctx, kKeys);
+  // the replicas arrive in sweep-axis order: a stable sort by list id alone
+  // (the key's high half) leaves every list sorted by its minima
   unsigned long long *kb[2] = {ctx->keys64[0].as<unsigned long long>(),
                                ctx->keys64[1].as<unsigned long long>()};
   uint32_t *vb[2] = {ctx->vals[0].as<uint32_t>(), ctx->vals[1].as<uint32_t>()};
   int which = 0;
   stage_begin(ctx, kSort);
   const int rbits = ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
-  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, ctx->rep_cap, 0, 32 + seg_bits,
-                                    ctx->sort_ws.ptr, &which, &ctx->launches, &b.hdr->replicas,
-                                    rbits),
-           "launch radix sort");
+  const int64_t r = replicas >= 0 ? replicas : ctx->rep_cap;
+  STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, r, 32, 32 + std::max(seg_bits, 1), ctx->sort_ws.ptr,
+                                    &which, &ctx->launches, &b.hdr->replicas, rbits),
+           "launch list sort");
   stage_end(ctx, kSort);
   ctx->scene.sx = ctx->sx.as<float2>();
   ctx->scene.syz = ctx->syz.as<float4>();
@@ -286,8 +316,8 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits) 
   stage_begin(ctx, kGather);
   STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, b.hdr, ctx->slot_cap),
            "launch sentinel fill");
-  STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, ctx->rep_cap,
-                                    b.cell_base, b.scenes, b.seg_count, b.seg_scan, ctx->scene),
+  STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, r, b.cell_base, b.scenes,
+                                    b.seg_count, b.seg_scan, ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
   ctx->launches += 4;
@@ -306,14 +336,14 @@ int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_
   fill_staging(ctx, box_off, S, axes, axis, nullptr, nullptr, nullptr);
   STQ_TRY(upload_staging(ctx));
   BatchBuffers b = batch_buffers(ctx, d_boxes);
-  STQ_TRY(enqueue_prepare_front(ctx, b));
+  STQ_TRY(enqueue_prepare_front(ctx, b, N));
   STQ_TRY(read_header(ctx));
   const int64_t R = ctx->h_hdr->replicas, cells = ctx->h_hdr->cells;
   if (R + 3 * cells + 1 + kSortedPad > int64_t(INT32_MAX))
     return fail(ctx, STQ_ERR_NO_MEMORY, "too many cell replicas for 32-bit positions");
   STQ_TRY(ensure_replica_buffers(ctx, std::max(R, ctx->rep_cap), cells));
   b = batch_buffers(ctx, d_boxes);
-  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * cells)));
+  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * cells), N, R));
   ctx->n_scenes = S;
   ctx->n_boxes = N;
   ctx->length = R > 0 ? R + 3 * cells - 1 : 0;
@@ -323,7 +353,7 @@ int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_
 }
 
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
-              long long capacity, bool count_mode) {
+              long long capacity, bool count_mode, bool reset, bool timed) {
   BatchHeader *hdr = dev_hdr(ctx);
   SweepParams p;
   p.sx = ctx->scene.sx;
@@ -346,11 +376,16 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
   p.hdr = hdr;
   p.stats = &hdr->candidates;
-  STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
-  stage_begin(ctx, count_mode ? kCountSweep : kSweep);
+  if (reset) {
+    STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
+    ctx->launches += 1;
+  } else {
+    STQ_CUDA(ctx, cudaMemsetAsync(&hdr->work, 0, sizeof(hdr->work), ctx->stream), "restart work cursor");
+  }
+  if (timed) stage_begin(ctx, count_mode ? kCountSweep : kSweep);
   STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
-  stage_end(ctx, count_mode ? kCountSweep : kSweep);
-  ctx->launches += 2;
+  if (timed) stage_end(ctx, count_mode ? kCountSweep : kSweep);
+  ctx->launches += 1;
   return STQ_OK;
 }
 
@@ -413,13 +448,21 @@ void stq_context_destroy(stq_context *ctx) {
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
                       &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->partner,
-                      &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws,
+                      &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
+                      &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
                       &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux})
       b->release();
     if (ctx->in_host) cudaFreeHost(ctx->in_host);
     if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
     if (ctx->h_scene_pairs) cudaFreeHost(ctx->h_scene_pairs);
+    if (ctx->copy_stream) {
+      cudaStreamSynchronize(ctx->copy_stream);
+      cudaStreamDestroy(ctx->copy_stream);
+    }
+    if (ctx->h_window_pairs) cudaFreeHost(ctx->h_window_pairs);
+    for (cudaEvent_t e : ctx->window_done)
+      if (e) cudaEventDestroy(e);
     for (int st = 0; st < kStages; ++st)
       for (int k = 0; k < 2; ++k)
         if (ctx->ev[st][k]) cudaEventDestroy(ctx->ev[st][k]);
@@ -434,7 +477,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 8 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 9 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -463,6 +506,9 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
     case STQ_OPT_GRAPH:
       if (value > 2) return fail(ctx, STQ_ERR_INVALID_ARG, "graph: 0 (default), 1 on, 2 off");
       break;
+    case STQ_OPT_HOST_OVERLAP:
+      if (value > 2) return fail(ctx, STQ_ERR_INVALID_ARG, "host overlap: 0 (default), 1 on, 2 off");
+      break;
     default:
       break;
   }
@@ -472,7 +518,7 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 8) return -1;
+  if (!ctx || option < 1 || option > 9) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
@@ -481,6 +527,7 @@ int64_t stq_context_get_option(const stq_context *ctx, int option) {
     case STQ_OPT_CELL_SCALE: return int64_t(ctx->cell_scale);
     case STQ_OPT_REPLICA_BUDGET: return ctx->budget;
     case STQ_OPT_GRAPH: return ctx->options[STQ_OPT_GRAPH] == 2 ? 2 : 1;
+    case STQ_OPT_HOST_OVERLAP: return ctx->options[STQ_OPT_HOST_OVERLAP] == 2 ? 2 : 1;
     default: return ctx->options[option];
   }
 }
@@ -493,6 +540,18 @@ int64_t stq_context_launch_count(const stq_context *ctx) { return ctx ? ctx->lau
 
 int64_t stq_context_candidates(const stq_context *ctx) {
   return ctx ? int64_t(ctx->h_hdr->candidates) : -1;
+}
+
+int stq_context_list_stats(stq_context *ctx, int64_t *out) {
+  if (!ctx || !out) return STQ_ERR_INVALID_ARG;
+  if (!ctx->prepared) return fail(ctx, STQ_ERR_NOT_PREPARED, "nothing prepared");
+  DeviceGuard g(ctx->device);
+  STQ_TRY(read_header(ctx));
+  const BatchHeader &h = *ctx->h_hdr;
+  out[0] = 3 * int64_t(h.cells);
+  out[1] = int64_t(h.replicas);
+  out[2] = int64_t(h.max_list);
+  return STQ_OK;
 }
 
 int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, int64_t nV,
@@ -714,8 +773,8 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
              "launch batched box build");
     stage_end(ctx, kBuild);
     const BatchBuffers b = batch_buffers(ctx, boxes);
-    STQ_TRY(enqueue_prepare_front(ctx, b));
-    STQ_TRY(enqueue_prepare_back(ctx, b, cell_bits));
+    STQ_TRY(enqueue_prepare_front(ctx, b, -1));
+    STQ_TRY(enqueue_prepare_back(ctx, b, cell_bits, -1, -1));
     STQ_TRY(run_sweep(ctx, 0, ctx->slot_cap, d_pairs, capacity, false));
     STQ_CUDA(ctx, cudaMemcpyAsync(ctx->h_hdr, dev_hdr(ctx), sizeof(BatchHeader),
                                   cudaMemcpyDeviceToHost, ctx->stream),
@@ -797,6 +856,91 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
   return found <= capacity ? STQ_OK : STQ_OVERFLOW;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Sweeps the prepared scene into h_pairs. The start positions are cut into
+// up to kCopyWindows windows swept one after another on the context's stream;
+// the pair counter runs on across windows, so window i's pairs are the range
+// [count after i-1, count after i) of one device buffer. Once a window's
+// event fires, the host reads its counter and queues the copy of that range
+// on a second stream: the copy engine moves window i to the host while the
+// SMs sweep window i+1, and the pair list's device-to-host transfer (the
+// largest cost of a host-buffer call) overlaps the sweep instead of
+// following it. An overflow (more pairs than capacity) falls back to the
+// prefix rule of stq_sweep_prepared and one copy.
+int sweep_to_host(stq_context *ctx, stq_pair *h_pairs, int64_t capacity, int64_t *count,
+                  int64_t *total) {
+  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1)),
+           "allocate pair staging");
+  stq_pair *d_pairs = ctx->e2e_pairs.as<stq_pair>();
+  const int64_t length = ctx->length;
+  constexpr int64_t kMinWindow = int64_t(1) << 19;  // start positions
+  const int windows = int(std::min<int64_t>(stq_context::kCopyWindows, length / kMinWindow));
+  auto copy_all = [&](int64_t c) -> int {
+    if (c <= 0) return STQ_OK;
+    STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, d_pairs, sizeof(stq_pair) * size_t(c), cudaMemcpyDeviceToHost,
+                                  ctx->stream),
+             "copy pairs to host");
+    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+    return STQ_OK;
+  };
+  if (windows < 2 || capacity == 0 || ctx->options[STQ_OPT_HOST_OVERLAP] == 2) {
+    int64_t next = 0;
+    const int st = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, count, &next, total);
+    if (st != STQ_OK && st != STQ_OVERFLOW) return st;
+    STQ_TRY(copy_all(*count));
+    return st;
+  }
+  if (!ctx->copy_stream)
+    STQ_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "create copy stream");
+  if (!ctx->h_window_pairs)
+    STQ_CUDA(ctx, cudaMallocHost(&ctx->h_window_pairs, sizeof(unsigned long long) * stq_context::kCopyWindows),
+             "allocate window counters");
+  for (int w = 0; w < windows; ++w)
+    if (!ctx->window_done[w])
+      STQ_CUDA(ctx, cudaEventCreateWithFlags(&ctx->window_done[w], cudaEventDisableTiming), "create event");
+  BatchHeader *hdr = dev_hdr(ctx);
+  stage_begin(ctx, kSweep);
+  for (int w = 0; w < windows; ++w) {
+    const int64_t b = length * w / windows, e = length * (w + 1) / windows;
+    STQ_TRY(run_sweep(ctx, b, e, d_pairs, capacity, false, w == 0, false));
+    STQ_CUDA(ctx, cudaMemcpyAsync(&ctx->h_window_pairs[w], &hdr->pairs, sizeof(unsigned long long),
+                                  cudaMemcpyDeviceToHost, ctx->stream),
+             "read window counter");
+    STQ_CUDA(ctx, cudaEventRecord(ctx->window_done[w], ctx->stream), "record window");
+  }
+  stage_end(ctx, kSweep);
+  int64_t done = 0;
+  for (int w = 0; w < windows; ++w) {
+    STQ_CUDA(ctx, cudaEventSynchronize(ctx->window_done[w]), "wait for sweep window");
+    const int64_t c = std::min<int64_t>(int64_t(ctx->h_window_pairs[w]), capacity);
+    if (c > done)
+      STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs + done, d_pairs + done, sizeof(stq_pair) * size_t(c - done),
+                                    cudaMemcpyDeviceToHost, ctx->copy_stream),
+               "copy window pairs to host");
+    done = std::max(done, c);
+  }
+  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream), "synchronise copy stream");
+  STQ_TRY(read_header(ctx));
+  const int64_t found = int64_t(ctx->h_hdr->pairs);
+  if (total) *total = found;
+  if (found <= capacity) {
+    *count = found;
+    return STQ_OK;
+  }
+  int64_t next = 0;
+  const int st = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, count, &next, total);
+  if (st != STQ_OK && st != STQ_OVERFLOW) return st;
+  STQ_TRY(copy_all(*count));
+  return st;
+}
+
+}  // namespace
+
+extern "C" {
+
 int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n, int axis,
                    stq_pair *h_pairs, int64_t capacity, int64_t *count, int64_t *total) {
   if (!ctx) return STQ_ERR_INVALID_ARG;
@@ -806,23 +950,12 @@ int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n, int axi
   DeviceGuard g(ctx->device);
   STQ_CUDA(ctx, ctx->e2e_boxes.ensure(sizeof(stq_aabb) * size_t(n > 0 ? n : 1)),
            "allocate box staging");
-  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1)),
-           "allocate pair staging");
   if (n > 0)
     STQ_CUDA(ctx, cudaMemcpyAsync(ctx->e2e_boxes.ptr, h_boxes, sizeof(stq_aabb) * size_t(n),
                                   cudaMemcpyHostToDevice, ctx->stream),
              "copy boxes to device");
-  int64_t next = 0;
-  const int st = stq_sweep(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis, 0, 0,
-                           ctx->e2e_pairs.as<stq_pair>(), capacity, count, &next, total);
-  if (st != STQ_OK && st != STQ_OVERFLOW) return st;
-  if (*count > 0) {
-    STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, ctx->e2e_pairs.ptr, sizeof(stq_pair) * size_t(*count),
-                                  cudaMemcpyDeviceToHost, ctx->stream),
-             "copy pairs to host");
-    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
-  }
-  return st;
+  STQ_TRY(stq_prepare(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis));
+  return sweep_to_host(ctx, h_pairs, capacity, count, total);
 }
 
 int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count) {
@@ -867,8 +1000,6 @@ int stq_broadphase_host(stq_context *ctx, const double *h_V0, const double *h_V1
   const int64_t n = nV + nE + nF;
   STQ_CUDA(ctx, ctx->e2e_boxes.ensure(sizeof(stq_aabb) * size_t(n > 0 ? n : 1)),
            "allocate box staging");
-  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1)),
-           "allocate pair staging");
   char *base = ctx->e2e_mesh.as<char>();
   if (bv) {
     STQ_CUDA(ctx, cudaMemcpyAsync(base, h_V0, bv, cudaMemcpyHostToDevice, ctx->stream), "copy V0");
@@ -882,16 +1013,7 @@ int stq_broadphase_host(stq_context *ctx, const double *h_V0, const double *h_V1
                           reinterpret_cast<const int32_t *>(base + oF), nF, inflation_radius,
                           ctx->e2e_boxes.as<stq_aabb>()));
   STQ_TRY(stq_prepare(ctx, ctx->e2e_boxes.as<stq_aabb>(), n, axis));
-  int64_t next = 0;
-  const int st = stq_sweep_prepared(ctx, 0, 0, ctx->e2e_pairs.as<stq_pair>(), capacity, count, &next, total);
-  if (st != STQ_OK && st != STQ_OVERFLOW) return st;
-  if (*count > 0) {
-    STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, ctx->e2e_pairs.ptr, sizeof(stq_pair) * size_t(*count),
-                                  cudaMemcpyDeviceToHost, ctx->stream),
-             "copy pairs to host");
-    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
-  }
-  return st;
+  return sweep_to_host(ctx, h_pairs, capacity, count, total);
 }
 
 int stq_context_enable_timing(stq_context *ctx, int enable) {

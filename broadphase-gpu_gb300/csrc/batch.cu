@@ -238,6 +238,17 @@ __device__ __forceinline__ Range cell_range(const stq_aabb &x, int a, float ob, 
 
 __device__ __forceinline__ float inv_side(int n, float L) { return n > 1 ? float(n) / L : 0.f; }
 
+// Scene of box bi: the last scene whose first box is <= bi.
+__device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, int S, uint32_t bi) {
+  int lo = 0, hi = S - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (box_off[mid] <= (long long)bi) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---- 3. replicas per grid level, per scene ------------------------------------------
 __global__ void __launch_bounds__(kBlock)
 batch_levels_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
@@ -341,19 +352,18 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
 
 // ---- 5. per-box replica counts (zero past the last box, up to the capacity) -----
 __global__ void __launch_bounds__(kBlock)
-batch_count_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
-                   const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
-                   uint32_t *__restrict__ counts, long long box_cap) {
+batch_count_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict__ order,
+                   const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
+                   const BatchHeader *hdr, uint32_t *__restrict__ counts, long long box_cap) {
   const long long N = hdr->n_boxes;
-  if (int(blockIdx.x) < hdr->n_tiles) {
-    const TileRec t = tiles[blockIdx.x];
-    const GridParams g = scenes[t.scene].grid;
-    for (int i = threadIdx.x; i < t.count; i += kBlock) {
-      const Range q = cell_range(boxes[t.begin + i], g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
-      counts[t.begin + i] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
-    }
+  const int S = hdr->n_scenes;
+  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
+    const uint32_t bi = order[p];
+    const GridParams g = scenes[scene_of(box_off, S, bi)].grid;
+    const Range q = cell_range(boxes[bi], g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
+    counts[p] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
   }
-  // boxes past the batch contribute nothing to the scan
+  // positions past the batch contribute nothing to the scan
   for (long long i = N + blockIdx.x * (long long)kBlock + threadIdx.x; i < box_cap;
        i += (long long)gridDim.x * kBlock)
     counts[i] = 0u;
@@ -363,41 +373,74 @@ batch_count_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
 // segment is (global cell, box type): every cell holds a vertex, an edge and
 // a face list. Also counts replicas per segment.
 __global__ void __launch_bounds__(kBlock)
-batch_emit_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
-                  const SceneRecord *__restrict__ scenes, const unsigned int *__restrict__ cell_base,
-                  BatchHeader *hdr, const uint32_t *__restrict__ offsets,
-                  unsigned long long *__restrict__ keys, uint32_t *__restrict__ vals,
-                  uint32_t *__restrict__ seg_count, long long rep_cap, long long seg_cap) {
+batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict__ order,
+                  const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
+                  const unsigned int *__restrict__ cell_base, BatchHeader *hdr,
+                  const uint32_t *__restrict__ offsets, unsigned long long *__restrict__ keys,
+                  uint32_t *__restrict__ vals, uint32_t *__restrict__ seg_count, long long rep_cap,
+                  long long seg_cap) {
   const bool fits = (long long)hdr->replicas <= rep_cap && 3ll * hdr->cells <= seg_cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // each of the 3 lists of a cell is followed by its sentinel; the last
     // sentinel is not a start position. On overflow nothing is emitted.
     hdr->length = fits && hdr->cells > 0 && hdr->replicas > 0 ? hdr->replicas + 3 * hdr->cells - 1 : 0u;
+    hdr->max_list = 0u;
     if (!fits) {
       atomicOr(&hdr->flags, kFlagReplicaOverflow);
       hdr->replicas = 0;
     }
   }
-  if (!fits || int(blockIdx.x) >= hdr->n_tiles) return;
-  const TileRec t = tiles[blockIdx.x];
-  const GridParams g = scenes[t.scene].grid;
-  const unsigned long long cb0 = cell_base[t.scene];
-  for (int i = threadIdx.x; i < t.count; i += kBlock) {
-    const long long bi = t.begin + i;
+  if (!fits) return;
+  const long long N = hdr->n_boxes;
+  const int S = hdr->n_scenes;
+  // positions in sweep-axis order: every list receives its replicas in key
+  // order, which the stable sort by list id keeps
+  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
+    const uint32_t bi = order[p];
+    const int sc = scene_of(box_off, S, bi);
+    const GridParams g = scenes[sc].grid;
+    const unsigned long long cb0 = cell_base[sc];
     const stq_aabb &x = boxes[bi];
     const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
     const unsigned long long xk = float_key(x.min[g.axis]);
     const unsigned long long type = type_of(x.vertex_ids[1], x.vertex_ids[2]);
-    uint32_t o = offsets[bi];
+    uint32_t o = offsets[p];
     for (int cb = q.b0; cb <= q.b1; ++cb)
       for (int cc = q.c0; cc <= q.c1; ++cc) {
         const unsigned long long seg = (cb0 + (unsigned long long)(cb * g.nc + cc)) * 3ull + type;
         keys[o] = (seg << 32) | xk;
-        vals[o] = uint32_t(bi);
+        vals[o] = bi;
         atomicAdd(&seg_count[seg], 1u);
         ++o;
       }
   }
+}
+
+// Sort keys of the boxes: the order-preserving image of the minimum on the
+// scene's sweep axis, with the box index as value.
+__global__ void __launch_bounds__(kBlock)
+batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
+                      const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
+                      uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+  if (int(blockIdx.x) >= hdr->n_tiles) return;
+  const TileRec t = tiles[blockIdx.x];
+  const int a = scenes[t.scene].grid.axis;
+  for (int i = threadIdx.x; i < t.count; i += kBlock) {
+    const long long bi = t.begin + i;
+    keys[bi] = float_key(boxes[bi].min[a]);
+    vals[bi] = uint32_t(bi);
+  }
+}
+
+// Longest (cell, type) list, a statistic of the prepared scene.
+__global__ void __launch_bounds__(kBlock)
+list_max_kernel(const uint32_t *__restrict__ seg_count, BatchHeader *__restrict__ hdr, long long seg_cap) {
+  // nothing was emitted past the capacity (the emit flags that overflow)
+  const uint32_t nseg = uint32_t(min(3ll * hdr->cells, seg_cap));
+  uint32_t mx = 0;
+  for (uint32_t s = blockIdx.x * kBlock + threadIdx.x; s < nseg; s += gridDim.x * kBlock) mx = max(mx, seg_count[s]);
+  mx = __reduce_max_sync(kFullMask, mx);
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&hdr->max_list, mx);
 }
 
 __global__ void __launch_bounds__(kBlock)
@@ -516,16 +559,22 @@ cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b) {
-  batch_count_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr,
-                                                             b.counts, b.box_cap);
+cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b) {
+  batch_box_keys_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr, b.box_keys,
+                                                                b.box_vals);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b) {
-  batch_emit_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.cell_base,
-                                                            b.hdr, b.offsets, b.keys, b.vals,
-                                                            b.seg_count, b.rep_cap, b.seg_cap);
+cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n) {
+  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.boxes, b.order, b.box_off, b.scenes, b.hdr, b.counts,
+                                               b.box_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms) {
+  batch_emit_kernel<<<blocks_for(n), kBlock, 0, s>>>(b.boxes, b.order, b.box_off, b.scenes, b.cell_base, b.hdr,
+                                              b.offsets, b.keys, b.vals, b.seg_count, b.rep_cap, b.seg_cap);
+  list_max_kernel<<<unsigned(num_sms * 2), kBlock, 0, s>>>(b.seg_count, b.hdr, b.seg_cap);
   return cudaGetLastError();
 }
 

@@ -76,6 +76,8 @@ struct stq_context {
   DevBuf scenes, cell_base, scene_pairs, counts, offsets, scan_ws, keys64[2], vals[2], sort_ws;
   DevBuf sx, syz, sv, sflag, partner, box_counts, prefix_ws, pair_keys[2];
   DevBuf seg_count, seg_scan, seg_scan_ws;  // replicas per (cell, type) list
+  DevBuf bkeys[2], bvals[2];  // box sort: keys and box indices, double-buffered
+  int order_buf = 0;          // which bvals buffer holds the sorted box order
   int64_t seg_cap = 0;
   DevBuf batch_boxes, e2e_boxes, e2e_pairs, e2e_mesh;
   DevBuf aux;  // header of calls outside a batch (box build, all-pairs check)
@@ -96,6 +98,13 @@ struct stq_context {
   cudaGraphExec_t graph = nullptr;
   GraphKey graph_key;
   bool capturing = false;
+
+  // host-buffer calls: copy stream, one event and one pinned pair counter per
+  // sweep window
+  static constexpr int kCopyWindows = 8;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t window_done[kCopyWindows] = {};
+  unsigned long long *h_window_pairs = nullptr;
 
   // autotuner cache: shape bucket -> options (lanes, queue, block, radix, scale)
   std::vector<std::pair<int64_t, std::vector<int64_t>>> tuned;
@@ -134,11 +143,21 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes);
 int ensure_box_buffers(stq_context *ctx, int64_t box_cap);
 int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap);
 int bits_for(int64_t v);
-int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b);
-// seg_bits: bits of the largest segment id (3 x cells)
-int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits);
+// Statistics, axis and grid per scene, the box sort along the sweep axis,
+// replica counts per sorted position and their scan. n_boxes: the box count,
+// or -1 when only the device knows it (graph capture, serving).
+int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_boxes);
+// Replica emit in sweep-axis order, list counts and offsets, and the stable
+// sort by list id (seg_bits bits) that turns it into x-sorted cell lists;
+// then the sorted scene. replicas: the replica count, or -1 (device count).
+int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, int64_t n_boxes,
+                         int64_t replicas);
+// reset: clear the pair counter, per-scene counts and statistics first (a
+// window of a longer sweep keeps them and only restarts the work cursor).
+// timed: record the launch as one sweep stage (a windowed caller times all
+// its windows as one).
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs, long long capacity,
-              bool count_mode);
+              bool count_mode, bool reset = true, bool timed = true);
 
 template <typename T>
 T *dev_at(stq_context *ctx, size_t off) {

@@ -243,10 +243,10 @@ size_t radix_workspace_bytes(int64_t n, int key_bytes, int bits) {
 
 cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
                            int64_t n, int bits, void *workspace, int *which,
-                           int64_t *launches) {
+                           int64_t *launches, const unsigned int *d_n) {
   if (bits == 4)
-    return sort_impl<uint32_t, 4, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches);
-  return sort_impl<uint32_t, 8, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches);
+    return sort_impl<uint32_t, 4, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches, d_n);
+  return sort_impl<uint32_t, 8, true>(s, kbuf, vbuf, n, 0, 32, workspace, which, launches, d_n);
 }
 
 cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2], int64_t n,

@@ -204,8 +204,8 @@ int enqueue_tick(stq_server *sv, bool advance) {
                                         ref_next_up(0.f), ctx->batch_boxes.as<stq_aabb>()),
            "launch box build");
   const BatchBuffers b = batch_buffers(ctx, ctx->batch_boxes.as<stq_aabb>());
-  STQ_TRY(enqueue_prepare_front(ctx, b));
-  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * (sv->max_boxes / 16 + sv->max_scenes + 1))));
+  STQ_TRY(enqueue_prepare_front(ctx, b, -1));
+  STQ_TRY(enqueue_prepare_back(ctx, b, bits_for(3 * (sv->max_boxes / 16 + sv->max_scenes + 1)), -1, -1));
   STQ_TRY(run_sweep(ctx, 0, ctx->slot_cap, sv->pairs.as<stq_pair>(), sv->pair_cap, false));
   STQ_CUDA(ctx, launch_pair_checksums(ctx->stream, sv->pairs.as<stq_pair>(), sv->pair_cap, hdr, box_off,
                                       sv->checks_dev.as<unsigned long long>(), sv->max_scenes),

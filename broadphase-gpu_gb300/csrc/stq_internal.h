@@ -112,7 +112,8 @@ struct BatchHeader {
   int axis;                 // sweep axis of scene 0
   int budget;               // replica budget: replicas <= budget * boxes per scene
   int n_tiles;              // input: entries of the tile table
-  int pad;
+  unsigned int max_list;    // longest (cell, type) list
+  unsigned int box_count;   // input: n_boxes as the element count of the box sort
   unsigned long long candidates;  // candidates tested by the last sweep
 };
 
@@ -191,7 +192,10 @@ struct BatchBuffers {
   SceneRecord *scenes;
   unsigned int *cell_base;      // n_scenes + 1
   BatchHeader *hdr;
-  uint32_t *counts, *offsets;   // per box
+  uint32_t *counts, *offsets;   // per box position in sweep-axis order
+  uint32_t *box_keys, *box_vals;  // box sort input (key, box index), double-buffered with
+  uint32_t *box_keys2, *box_vals2;
+  const uint32_t *order;        // boxes in sweep-axis order (box sort output)
   unsigned long long *keys;     // replica keys (sort input)
   uint32_t *vals;               // replica box indices (sort input)
   uint32_t *seg_count;          // replicas per segment (cell x type), seg_cap entries
@@ -203,8 +207,12 @@ struct BatchBuffers {
 };
 cudaError_t launch_batch_stats(cudaStream_t s, const BatchBuffers &b);
 cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b);
-cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b);
-cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b);
+cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b);
+// n: positions to cover (the box count, or the box capacity when only the
+// device knows the count)
+cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n);
+cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms);
+
 cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, const BatchHeader *hdr,
                                   int64_t slots_cap);
 cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
@@ -245,7 +253,7 @@ cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long l
 size_t radix_workspace_bytes(int64_t n, int key_bytes, int bits);
 cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
                            int64_t n, int bits, void *workspace, int *which,
-                           int64_t *launches);
+                           int64_t *launches, const unsigned int *d_n = nullptr);
 cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2],
                            int64_t n, int begin_bit, int end_bit, void *workspace,
                            int *which, int64_t *launches);

@@ -42,7 +42,7 @@ STQ_ERR_NOT_PREPARED = -7
 
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
 OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
-OPT_REPLICA_BUDGET, OPT_GRAPH = 7, 8
+OPT_REPLICA_BUDGET, OPT_GRAPH, OPT_HOST_OVERLAP = 7, 8, 9
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
@@ -59,6 +59,7 @@ ABI_SIGNATURES = {
     "stq_context_last_error": (ctypes.c_char_p, [_vp]),
     "stq_context_launch_count": (ctypes.c_int64, [_vp]),
     "stq_context_candidates": (ctypes.c_int64, [_vp]),
+    "stq_context_list_stats": (ctypes.c_int, [_vp, _vp]),
     "stq_build_boxes": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64,
                                        _vp, ctypes.c_int64, ctypes.c_float, _vp]),
     "stq_select_axis": (ctypes.c_int, [_vp, _vp, ctypes.c_int64, ctypes.POINTER(ctypes.c_int)]),
@@ -209,6 +210,12 @@ class Context:
     def candidates(self) -> int:
         """Candidates the last sweep tested."""
         return int(self.lib.stq_context_candidates(self._h))
+
+    def list_stats(self) -> dict:
+        """(cell, type) lists of the prepared scene: count, replicas, longest."""
+        out = np.zeros(3, np.int64)
+        self._check(self.lib.stq_context_list_stats(self._h, out.ctypes.data))
+        return dict(zip(("lists", "replicas", "longest"), (int(v) for v in out)))
 
     @property
     def launches(self) -> int:

@@ -89,11 +89,15 @@ typedef enum stq_option {
                                   1 no cells (plain sweep), k > 1 a k x k grid      */
   STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
   STQ_OPT_CELL_SCALE = 6,      /* automatic cell side in median box extents (1..64,
-                                  default 4)                                        */
+                                  default 2)                                        */
   STQ_OPT_REPLICA_BUDGET = 7,  /* cell replicas per box a scene may use (1..64,
                                   default 4); finer grids beyond it are coarsened   */
-  STQ_OPT_GRAPH = 8            /* stq_batch_broadphase: 1 capture and replay a CUDA
+  STQ_OPT_GRAPH = 8,           /* stq_batch_broadphase: 1 capture and replay a CUDA
                                   graph (default), 2 plain stream launches          */
+  STQ_OPT_HOST_OVERLAP = 9     /* stq_sweep_host / stq_broadphase_host: 1 sweep in
+                                  windows, each window's pairs copied to the host
+                                  while the next is swept (default), 2 one copy
+                                  after the whole sweep                            */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -114,6 +118,9 @@ int64_t stq_context_launch_count(const stq_context *ctx);
 /* Candidates (x-overlapping start box / candidate pairs) the last sweep
  * tested, a measure of the sweep's work beyond the pairs it found. */
 int64_t stq_context_candidates(const stq_context *ctx);
+/* Shape of the prepared scene's (cell, type) lists: out[0] lists (3 per
+ * cell), out[1] cell replicas, out[2] the longest list. Synchronises. */
+int stq_context_list_stats(stq_context *ctx, int64_t out[3]);
 
 /* Swept boxes from vertex trajectories. d_V0/d_V1 are row-major [nV x 3]
  * fp64 positions at t0 and t1, d_E [nE x 2] and d_F [nF x 3] int32 vertex
@@ -161,7 +168,12 @@ int stq_sweep(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis,
 
 /* End-to-end call on host memory: copies h_boxes to the device, sweeps all
  * start boxes, copies the pairs back to h_pairs (capacity entries). Same
- * return codes as stq_sweep; on STQ_OVERFLOW h_pairs holds the prefix. */
+ * return codes as stq_sweep; on STQ_OVERFLOW h_pairs holds the prefix.
+ * Scenes of 2^20 or more sweep positions are swept in windows of start
+ * positions; each window's pairs are copied to h_pairs on a second stream
+ * while the next window is swept (STQ_OPT_HOST_OVERLAP = 2: one copy after the
+ * sweep). A page-locked h_pairs (cudaHostAlloc / cudaHostRegister) lets those
+ * copies run asynchronously. The same holds for stq_broadphase_host. */
 int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n,
                    int axis, stq_pair *h_pairs, int64_t capacity,
                    int64_t *count, int64_t *total);

@@ -311,6 +311,68 @@ def test_sweep_host_end_to_end(stq, oracle, cuda, c0):
         assert ctx.launches > 0
 
 
+@pytest.fixture(scope="module")
+def big_cloth(stq):
+    """Cloth pair of 2 x 450^2 vertices (about 2.4 M boxes): large enough for
+    the host calls to sweep in windows."""
+    return stq.cloth_pair(g=450, seed=3)
+
+
+@pytest.mark.parametrize("overlap", [1, 2])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, overlap, pinned):
+    """Host calls sweep large scenes in windows whose pair ranges are copied
+    while the next window runs (OPT_HOST_OVERLAP=1) or copy once after the
+    sweep (=2); both give the device sweep's pairs, into page-locked or
+    pageable buffers, and the overflow prefix of the one-window path."""
+    import torch
+
+    m = big_cloth
+    alloc = ((lambda shape: torch.empty(shape, dtype=torch.int32).pin_memory().numpy()) if pinned
+             else (lambda shape: np.empty(shape, np.int32)))
+    with stq.Context(0) as ctx:
+        d = [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in (m.V0, m.V1, m.E, m.F)]
+        boxes = torch.empty((m.num_boxes, 11), dtype=torch.int32, device=cuda)
+        ctx.build_boxes(*d, boxes)
+        ctx.prepare(boxes, m.num_boxes, stq.AXIS_AUTO)
+        length = ctx.prepared_length
+        assert length >= 2 << 19
+        cap = 64 * m.num_boxes
+        dp = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+        r = ctx.sweep_prepared(dp, cap)
+        want = oracle.canonical(dp[: r.count].cpu().numpy())
+        ctx.set_option(stq.OPT_HOST_OVERLAP, overlap)
+        assert ctx.get_option(stq.OPT_HOST_OVERLAP) == overlap
+        out = alloc((len(want) + 10, 2))
+        for _ in range(2):  # the buffers are reused: no stale pairs
+            out[:] = -7
+            l0 = ctx.launches
+            r = ctx.broadphase_host(m, out, stq.AXIS_AUTO)
+            launches = ctx.launches - l0
+            assert r.status == stq.STQ_OK and r.count == len(want)
+            got = oracle.canonical(out[: r.count])
+            assert len(got) == r.count and np.array_equal(got, want)
+            assert (out[r.count:] == -7).all()
+        # the windowed call launches one sweep per window instead of one
+        ctx.set_option(stq.OPT_HOST_OVERLAP, 3 - overlap)
+        l0 = ctx.launches
+        ctx.broadphase_host(m, out, stq.AXIS_AUTO)
+        other = ctx.launches - l0
+        ctx.set_option(stq.OPT_HOST_OVERLAP, overlap)
+        windows = min(8, length >> 19)
+        assert launches - other == (windows - 1 if overlap == 1 else 1 - windows)
+        hb = boxes.cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
+        r = ctx.sweep_host(hb, out)
+        assert r.status == stq.STQ_OK and np.array_equal(oracle.canonical(out[: r.count]), want)
+        # overflow: the windows' pairs do not fit; the result is the prefix rule's
+        small = alloc((len(want) // 3, 2))
+        rs = ctx.sweep_host(hb, small)
+        ref = ctx.sweep_prepared(dp, len(want) // 3)
+        assert rs.status == ref.status == stq.STQ_OVERFLOW and rs.total == len(want)
+        assert rs.count == ref.count
+        assert np.array_equal(oracle.canonical(small[: rs.count]), oracle.canonical(dp[: ref.count].cpu().numpy()))
+
+
 def test_prepared_scene_reused_across_windows(ctx, stq, oracle, cuda, c0):
     import torch
 
@@ -329,7 +391,7 @@ def test_prepared_scene_reused_across_windows(ctx, stq, oracle, cuda, c0):
 
 # ---- cells (y/z grid segmentation with reference-point dedup) -------------------------
 
-@pytest.mark.parametrize("cells", [1, 2, 3, 7, 64, 512])
+@pytest.mark.parametrize("cells", [1, 2, 3, 7, 12, 16, 24, 64, 512])
 def test_cells_fixed_grids(ctx, stq, oracle, cuda, c0, cells):
     m, boxes, want = c0
     ctx.set_option(stq.OPT_CELLS, cells)
@@ -338,6 +400,29 @@ def test_cells_fixed_grids(ctx, stq, oracle, cuda, c0, cells):
         assert np.array_equal(got, want), (cells, axis)
         if cells == 1:
             assert ctx.prepared_length == len(boxes) + 2
+
+
+@pytest.mark.parametrize("cells", [3, 5, 8, 11])
+@pytest.mark.parametrize("ties", [False, True])
+def test_list_order_vs_oracle(ctx, stq, oracle, cuda, cells, ties):
+    """Lists of a few hundred to about ten thousand replicas, with and
+    without many equal minima: boxes sorted along the sweep axis, replicas
+    emitted in that order, then a stable sort by list id, with 8- and 4-bit
+    digits. list_stats reports the grid's lists."""
+    boxes = stq.random_boxes(120_000, seed=20 + cells)
+    c = 0.5 * (boxes["min"] + boxes["max"])
+    boxes["min"], boxes["max"] = c - 0.004, c + 0.004
+    if ties:
+        boxes["min"][:, 0] = np.round(boxes["min"][:, 0] * 64) / 64
+    want = oracle.broadphase(boxes)
+    ctx.set_option(stq.OPT_CELLS, cells)
+    for radix in (8, 4):
+        ctx.set_option(stq.OPT_RADIX_BITS, radix)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
+        assert np.array_equal(got, want), radix
+        stats = ctx.list_stats()
+        assert stats["lists"] == 3 * cells * cells and stats["replicas"] >= len(boxes)
+        assert stats["longest"] > stats["replicas"] // stats["lists"]
 
 
 @pytest.mark.parametrize("scale", [1, 2, 4, 16])
