@@ -72,29 +72,37 @@ def ncu_traffic(kernel: str, workload: str):
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks and throttle reasons, sampled every 20 ms from before the
+    warm-up (its start-up stays out of the timed region); the summary keeps the
+    samples whose timestamps fall inside the marked timed region."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, index: int):
         self.index = index
         self.proc = None
+        self.out = ""
+        self.window = None
 
-    def __enter__(self):
+    def start(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.5)  # let it initialise before anything is timed
         except (FileNotFoundError, OSError):
             self.proc = None
         return self
 
-    def __exit__(self, *exc):
-        self.out = ""
+    def mark(self, t0, t1):
+        self.window = (t0, t1)
+
+    def stop(self):
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             try:
                 self.out, _ = self.proc.communicate(timeout=5)
@@ -103,20 +111,29 @@ class ClockSampler:
                 self.out, _ = self.proc.communicate()
 
     def summary(self):
+        import datetime
+
         rows = []
         for line in (self.out or "").splitlines():
             f = [x.strip() for x in line.split(",")]
-            if len(f) >= 9:
+            if len(f) >= 10:
                 try:
-                    rows.append((float(f[1]), float(f[2]), f[5:9]))
+                    ts = datetime.datetime.strptime(f[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                    rows.append((ts, float(f[2]), float(f[3]), f[6:10]))
                 except ValueError:
                     pass
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        inside = rows
+        if self.window:
+            t0, t1 = self.window
+            inside = [r for r in rows if t0 - 0.02 <= r[0] <= t1 + 0.02]
+            if not inside:  # region shorter than the sampling period: the nearest sample
+                inside = [min(rows, key=lambda r: abs(r[0] - 0.5 * (t0 + t1)))]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, r in rows for i in range(4) if r[i].lower() == "active"})
-        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+        reasons = sorted({names[i] for _, _, _, r in inside for i in range(4) if r[i].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[1] for r in inside), "sm_max_mhz": max(r[2] for r in inside),
+                "reasons": reasons, "samples": len(inside)}
 
 
 def cpu_baseline(stq, orc, boxes, budget_s: float, threads: int = 0):
@@ -269,7 +286,7 @@ def run_reference(args, w):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="stq", choices=["stq", "reference"])
     ap.add_argument("--workload", default="crumpled16x250", choices=sorted(WORKLOADS))
@@ -344,6 +361,7 @@ def main():
         assert res.status == stq.STQ_OK, res
         return res.count
 
+    clk = ClockSampler(local).start()
     for _ in range(args.warmup):
         flush.fill_(1)
         step()
@@ -355,14 +373,16 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
-    with ClockSampler(local) as clk:
-        for i in range(args.steps):
-            with torch.cuda.stream(stream):
-                flush.fill_(i)  # evict the previous step's working set from L2
-            evs[i][0].record(stream)
-            npairs = step()
-            evs[i][1].record(stream)
-        torch.cuda.synchronize(dev)
+    t_region = time.time()
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)  # evict the previous step's working set from L2
+        evs[i][0].record(stream)
+        npairs = step()
+        evs[i][1].record(stream)
+    torch.cuda.synchronize(dev)
+    clk.mark(t_region, time.time())
+    clk.stop()
     if dist:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]

@@ -73,6 +73,8 @@ void apply_options(stq_context *ctx) {
   if (ctx->options[STQ_OPT_LANES_PER_ENTRY]) t.lanes = int(ctx->options[STQ_OPT_LANES_PER_ENTRY]);
   if (ctx->options[STQ_OPT_QUEUE_DEPTH]) t.queue = int(ctx->options[STQ_OPT_QUEUE_DEPTH]);
   if (ctx->options[STQ_OPT_BLOCK_SIZE]) t.block = int(ctx->options[STQ_OPT_BLOCK_SIZE]);
+  if (ctx->options[STQ_OPT_CANDIDATES_PER_LANE]) t.per_lane = int(ctx->options[STQ_OPT_CANDIDATES_PER_LANE]);
+  if (ctx->options[STQ_OPT_RUN_CAP]) t.run_cap = int(ctx->options[STQ_OPT_RUN_CAP]);
   ctx->tuning = t;
   ctx->cell_scale = ctx->options[STQ_OPT_CELL_SCALE] ? float(ctx->options[STQ_OPT_CELL_SCALE]) : 2.f;
   ctx->budget = ctx->options[STQ_OPT_REPLICA_BUDGET] ? int(ctx->options[STQ_OPT_REPLICA_BUDGET]) : 4;
@@ -243,6 +245,7 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
   STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->partner.ensure(sizeof(int) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->long_list.ensure(sizeof(int2) * slots), "allocate long-run list");
   ctx->rep_cap = int64_t(r);
   ctx->slot_cap = int64_t(slots);
   return STQ_OK;
@@ -352,6 +355,10 @@ int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_
   return STQ_OK;
 }
 
+static_assert(offsetof(BatchHeader, long_items) == offsetof(BatchHeader, work) + sizeof(int) &&
+                  offsetof(BatchHeader, long_work) == offsetof(BatchHeader, work) + 2 * sizeof(int),
+              "the sweep cursors are cleared as one block");
+
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
               long long capacity, bool count_mode, bool reset, bool timed) {
   BatchHeader *hdr = dev_hdr(ctx);
@@ -376,11 +383,18 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
   p.hdr = hdr;
   p.stats = &hdr->candidates;
+  p.typed = 1;
+  p.run_cap = ctx->tuning.run_cap;
+  p.long_list = ctx->long_list.as<int2>();
+  p.long_items = &hdr->long_items;
+  p.long_work = &hdr->long_work;
   if (reset) {
     STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
     ctx->launches += 1;
   } else {
-    STQ_CUDA(ctx, cudaMemsetAsync(&hdr->work, 0, sizeof(hdr->work), ctx->stream), "restart work cursor");
+    // work cursor and the warp pass's list and cursor (adjacent in the header)
+    STQ_CUDA(ctx, cudaMemsetAsync(&hdr->work, 0, sizeof(int) + 2 * sizeof(unsigned int), ctx->stream),
+             "restart work cursors");
   }
   if (timed) stage_begin(ctx, count_mode ? kCountSweep : kSweep);
   STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
@@ -447,7 +461,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
-                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->partner,
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->partner, &ctx->long_list,
                       &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
@@ -477,7 +491,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 9 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 11 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -509,6 +523,12 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
     case STQ_OPT_HOST_OVERLAP:
       if (value > 2) return fail(ctx, STQ_ERR_INVALID_ARG, "host overlap: 0 (default), 1 on, 2 off");
       break;
+    case STQ_OPT_CANDIDATES_PER_LANE:
+      if (!pow2_in(value, 1, 8)) return fail(ctx, STQ_ERR_INVALID_ARG, "candidates per lane: 1, 2, 4 or 8");
+      break;
+    case STQ_OPT_RUN_CAP:
+      if (value > (int64_t(1) << 20)) return fail(ctx, STQ_ERR_INVALID_ARG, "run cap: 1..2^20");
+      break;
     default:
       break;
   }
@@ -518,7 +538,7 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 9) return -1;
+  if (!ctx || option < 1 || option > 11) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
@@ -528,6 +548,8 @@ int64_t stq_context_get_option(const stq_context *ctx, int option) {
     case STQ_OPT_REPLICA_BUDGET: return ctx->budget;
     case STQ_OPT_GRAPH: return ctx->options[STQ_OPT_GRAPH] == 2 ? 2 : 1;
     case STQ_OPT_HOST_OVERLAP: return ctx->options[STQ_OPT_HOST_OVERLAP] == 2 ? 2 : 1;
+    case STQ_OPT_CANDIDATES_PER_LANE: return ctx->tuning.per_lane;
+    case STQ_OPT_RUN_CAP: return ctx->tuning.run_cap;
     default: return ctx->options[option];
   }
 }
@@ -1053,11 +1075,12 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   *best_ms = 0.0;
   const int64_t key = (int64_t(bits_for(std::max<int64_t>(h_box_off[n_scenes], 1))) << 32) |
                       int64_t(bits_for(n_scenes));
-  const int opts[5] = {STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH, STQ_OPT_BLOCK_SIZE,
-                       STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE};
+  constexpr int kOpts = 6;
+  const int opts[kOpts] = {STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH, STQ_OPT_BLOCK_SIZE,
+                           STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE, STQ_OPT_CANDIDATES_PER_LANE};
   for (const auto &kv : ctx->tuned)
     if (kv.first == key) {
-      for (int o = 0; o < 5; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], kv.second[size_t(o)]));
+      for (int o = 0; o < kOpts; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], kv.second[size_t(o)]));
       return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO);
     }
   const bool was_timing = ctx->timing;
@@ -1079,7 +1102,10 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
     *ms = best;
     return STQ_OK;
   };
-  std::vector<int64_t> best_set(5, 0);
+  std::vector<int64_t> best_set(kOpts, 0);
+  // sweep shapes: one start box per lane with 2, 4 or 8 candidates per step,
+  // or lane groups of 4, 8 or 16 lanes sharing one start box
+  const int64_t shapes[6][2] = {{1, 2}, {1, 4}, {1, 8}, {4, 0}, {8, 0}, {16, 0}};
   float best_total = 1e30f;
   int st = STQ_OK;
   for (int64_t scale : {1, 2, 4}) {
@@ -1090,10 +1116,12 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
       st = elapsed([&] { return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO); },
                    &t_prep);
       if (st != STQ_OK) break;
-      for (int64_t lanes : {4, 8, 16, 32})
+      for (const auto &shape : shapes)
         for (int64_t queue : {32, 64, 128})
           for (int64_t block : {128, 256, 512}) {
+            const int64_t lanes = shape[0], per_lane = shape[1];
             stq_context_set_option(ctx, STQ_OPT_LANES_PER_ENTRY, lanes);
+            stq_context_set_option(ctx, STQ_OPT_CANDIDATES_PER_LANE, per_lane);
             stq_context_set_option(ctx, STQ_OPT_QUEUE_DEPTH, queue);
             stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, block);
             float t_sweep = 0.f;
@@ -1105,7 +1133,7 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
             if (st != STQ_OK) break;
             if (t_prep + t_sweep < best_total) {
               best_total = t_prep + t_sweep;
-              best_set = {lanes, queue, block, radix, scale};
+              best_set = {lanes, queue, block, radix, scale, per_lane};
             }
           }
       if (st != STQ_OK) break;
@@ -1116,7 +1144,7 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   cudaEventDestroy(e1);
   ctx->timing = was_timing;
   if (st != STQ_OK) return st;
-  for (int o = 0; o < 5; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], best_set[size_t(o)]));
+  for (int o = 0; o < kOpts; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], best_set[size_t(o)]));
   ctx->tuned.emplace_back(key, best_set);
   *best_ms = double(best_total);
   return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO);

@@ -533,6 +533,8 @@ reset_sweep_kernel(BatchHeader *hdr, unsigned long long *scene_pairs) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     hdr->pairs = 0ull;
     hdr->work = 0;
+    hdr->long_items = 0u;
+    hdr->long_work = 0u;
     hdr->candidates = 0ull;
   }
 }

@@ -75,6 +75,7 @@ struct stq_context {
   size_t in_host_bytes = 0;
   DevBuf scenes, cell_base, scene_pairs, counts, offsets, scan_ws, keys64[2], vals[2], sort_ws;
   DevBuf sx, syz, sv, sflag, partner, box_counts, prefix_ws, pair_keys[2];
+  DevBuf long_list;  // runs handed from the lane sweep to the warp pass
   DevBuf seg_count, seg_scan, seg_scan_ws;  // replicas per (cell, type) list
   DevBuf bkeys[2], bvals[2];  // box sort: keys and box indices, double-buffered
   int order_buf = 0;          // which bvals buffer holds the sorted box order

@@ -150,6 +150,11 @@ extern "C" int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, st
   p.scene_pairs = reinterpret_cast<unsigned long long *>(scratch + kOffScenePairs);
   p.hdr = hdr;
   p.stats = nullptr;
+  p.typed = 0;  // one list of all box types
+  p.run_cap = 0;  // no warp pass: it would need a list of handed-over runs
+  p.long_list = nullptr;
+  p.long_items = nullptr;
+  p.long_work = nullptr;
   int num_sms = 152;
   cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (launch_sweep(s, p, SweepTuning(), false, num_sms) != cudaSuccess) return STQ_ERR_CUDA;

@@ -22,7 +22,7 @@ static_assert(offsetof(stq_aabb, min) == 4 && offsetof(stq_aabb, max) == 16 &&
 constexpr unsigned kFullMask = 0xffffffffu;
 // Padding after the last sentinel of a sorted scene, so that a lane group of
 // up to 32 lanes may read past a run end without leaving the allocation.
-constexpr int kSortedPad = 64;
+constexpr int kSortedPad = 256;
 
 // ---- IEEE next float, as the reference calls it -----------------------------
 // nextafter_up(x) = nextafterf(x, x + FLT_MAX) and nextafter_down(x) =

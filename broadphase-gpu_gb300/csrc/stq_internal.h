@@ -107,6 +107,8 @@ struct BatchHeader {
   unsigned int cells;       // total cells of all scenes
   unsigned int length;      // sweep positions: R + 3 * cells - 1
   int work;                 // sweep grab cursor
+  unsigned int long_items;  // runs handed from the lane sweep to the warp pass
+  unsigned int long_work;   // warp pass grab cursor
   unsigned long long pairs; // pairs found by the last sweep
   long long prefix;         // overflow: start positions of the prefix that fits
   int axis;                 // sweep axis of scene 0
@@ -128,7 +130,9 @@ struct TileRec {
 
 // Sweep-kernel tuning (autotuned or set through stq_context_set_option).
 struct SweepTuning {
-  int lanes = 8;        // lanes sharing one pending start box (1..32)
+  int lanes = 1;        // lanes sharing one pending start box (1..32)
+  int per_lane = 8;     // lanes = 1: candidates a lane tests per step (1, 2, 4, 8)
+  int run_cap = 512;    // candidates per start box before the warp pass takes over
   int queue = 64;       // warp queue depth (32, 64, 128)
   int block = 256;      // threads per block (128, 256, 512)
   int chunk = 256;      // start boxes per work grab
@@ -161,6 +165,14 @@ struct SweepParams {
   unsigned long long *scene_pairs;  // per-scene pair counters
   const BatchHeader *hdr;    // device sizes (length bounds the sweep range)
   unsigned long long *stats; // candidates tested (may be null)
+  int typed;                 // every list holds one box type, so every candidate
+                             // pair is V-F, F-V or E-E (is_valid_pair holds)
+  int run_cap;               // candidates of one start box a lane (group) tests
+                             // before it hands the rest of the run to the warp
+                             // pass; 0 = never
+  int2 *long_list;           // handed-over runs (start position, next candidate)
+  unsigned int *long_items;  // their count
+  unsigned int *long_work;   // warp pass grab cursor
 };
 
 // ---- launch wrappers (each returns the launch error) -------------------------

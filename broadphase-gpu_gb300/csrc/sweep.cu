@@ -58,7 +58,7 @@ stq_sweep_kernel(const SweepParams p) {
   int next_k = 0, chunk_end = 0;
   bool more = true;
   // lane-group state (identical in the G lanes of a group)
-  int k = -1, j0 = 0, acc = 0;
+  int k = -1, j0 = 0, acc = 0, taken = 0;
   float kmax = 0.f;
   float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
   int4 kv = make_int4(0, 0, 0, 0);
@@ -71,6 +71,7 @@ stq_sweep_kernel(const SweepParams p) {
   int staged = 0;
   int wscene = 0;
   unsigned long long wpairs = 0;
+  const bool multi = p.hdr->n_scenes > 1;  // per-scene counts need the scene of each hit
   int2 *st = stage[COUNT ? 0 : (threadIdx.x >> 5)];
 
   while (true) {
@@ -110,6 +111,7 @@ stq_sweep_kernel(const SweepParams p) {
         kb = p.syz[k];
         kv = p.sv[k];
         acc = 0;
+        taken = 0;
         kf = p.sflag[k];
       }
     }
@@ -134,7 +136,7 @@ stq_sweep_kernel(const SweepParams p) {
       const float4 b = p.syz[j];
       if (overlap_bc(kb, b)) {  // ids only for candidates that overlap on b and c
         const int4 bv = p.sv[j];
-        hit = valid_pair(kv, bv) && !covertex(kv, bv);
+        hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
       // a pair found in several cells is emitted only in the cell of its
       // reference point: on b and on c, one of the two replicas must be its
       // box's first cell (the candidate's bits are read only when needed)
@@ -153,16 +155,20 @@ stq_sweep_kernel(const SweepParams p) {
       if (hit) st[staged + __popc(hm & lanemask_lt())] = make_int2(lo_id, hi_id);
       staged += __popc(hm);
       // per-scene counts: one register while the warp stays in one scene
-      const int lead = __shfl_sync(kFullMask, kf >> 2, __ffs(hm) - 1);
-      if (__all_sync(kFullMask, !hit || (kf >> 2) == lead)) {
-        if (lead != wscene) {
-          if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
-          wscene = lead;
-          wpairs = 0;
-        }
+      if (!multi) {
         wpairs += __popc(hm);
-      } else if (gl == 0 && ghits) {
-        atomicAdd(&p.scene_pairs[kf >> 2], (unsigned long long)ghits);
+      } else {
+        const int lead = __shfl_sync(kFullMask, kf >> 2, __ffs(hm) - 1);
+        if (__all_sync(kFullMask, !hit || (kf >> 2) == lead)) {
+          if (lead != wscene) {
+            if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+            wscene = lead;
+            wpairs = 0;
+          }
+          wpairs += __popc(hm);
+        } else if (gl == 0 && ghits) {
+          atomicAdd(&p.scene_pairs[kf >> 2], (unsigned long long)ghits);
+        }
       }
       if (staged >= 32) {
         __syncwarp();
@@ -175,6 +181,14 @@ stq_sweep_kernel(const SweepParams p) {
     if (active) {
       if ((vm & grp_mask) == grp_mask) {
         j0 += G;
+        taken += G;
+        if (p.run_cap && taken >= p.run_cap) {  // a long run: the warp pass takes the rest
+          if (gl == 0) {
+            p.long_list[atomicAdd(p.long_items, 1u)] = make_int2(k, j0);
+            if (COUNT) p.box_counts[k - p.begin] = acc;
+          }
+          k = -1;
+        }
       } else {
         if (COUNT && gl == 0) p.box_counts[k - p.begin] = acc;
         k = -1;
@@ -190,34 +204,298 @@ stq_sweep_kernel(const SweepParams p) {
   }
 }
 
-template <int G, int Q, int BLOCK, bool COUNT>
-cudaError_t launch_variant(cudaStream_t s, const SweepParams &p, int num_sms) {
+// One start box per lane. A lane walks its own run, U consecutive candidates
+// per step: the U minima are loaded together (U independent loads in flight
+// per lane), the valid ones are the prefix before the first x-test failure
+// (lane-local: no ballot), and a lane whose run ended takes the next pending
+// box from the warp's ring. Otherwise as stq_sweep_kernel: ring refill by
+// ballot compaction, lazy vertex-id loads, per-warp staging of pairs.
+template <int U, int Q, int BLOCK, bool COUNT>
+__global__ void __launch_bounds__(BLOCK)
+stq_sweep_lane_kernel(const SweepParams p) {
+  static_assert(U == 1 || U == 2 || U == 4 || U == 8, "candidates per lane step: 1, 2, 4 or 8");
+  static_assert((Q & (Q - 1)) == 0 && Q >= 32, "queue depth: power of two >= 32");
+  constexpr int STAGE = 32 * (U + 1);  // < 32 left over + at most 32 * U new pairs
+  __shared__ int ring[BLOCK / 32][Q];
+  __shared__ int2 stage[COUNT ? 1 : BLOCK / 32][COUNT ? 1 : STAGE];
+
+  const int lane = threadIdx.x & 31;
+  const unsigned below = lanemask_lt();
+  int *q = ring[threadIdx.x >> 5];
+  int2 *st = stage[COUNT ? 0 : (threadIdx.x >> 5)];
+
+  int qhead = 0, qsize = 0;
+  int next_k = 0, chunk_end = 0;
+  bool more = true;
+  int k = -1, j = 0, acc = 0, kf = 0, taken = 0;
+  float kmax = 0.f;
+  float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
+  int4 kv = make_int4(0, 0, 0, 0);
+  const int end = min(p.end, int(p.hdr->length));
+  const int span = end - p.begin;
+  unsigned tested = 0;
+  int staged = 0;
+  int wscene = 0;
+  unsigned long long wpairs = 0;
+  const bool multi = p.hdr->n_scenes > 1;
+
+  while (true) {
+    // 1. Refill the ring with start boxes that have at least one candidate.
+    while (qsize < 32 && more) {
+      if (next_k >= chunk_end) {
+        int c = 0;
+        if (lane == 0) c = atomicAdd(p.work, p.chunk);
+        c = __shfl_sync(kFullMask, c, 0);
+        if (c >= span) {
+          more = false;
+          break;
+        }
+        next_k = p.begin + c;
+        chunk_end = min(next_k + p.chunk, end);
+      }
+      const int take = min(32, min(Q - qsize, chunk_end - next_k));
+      const int kk = next_k + lane;
+      bool push = false;
+      if (lane < take) push = p.sx[p.partner[kk]].x <= p.sx[kk].y;
+      const unsigned m = __ballot_sync(kFullMask, push);
+      if (push) q[(qhead + qsize + __popc(m & below)) & (Q - 1)] = kk;
+      qsize += __popc(m);
+      next_k += take;
+    }
+    __syncwarp();
+    // 2. Idle lanes take pending start boxes, in ring order.
+    const unsigned needm = __ballot_sync(kFullMask, k < 0);
+    const int ntake = min(__popc(needm), qsize);
+    if (k < 0) {
+      const int r = __popc(needm & below);
+      if (r < ntake) {
+        k = q[(qhead + r) & (Q - 1)];
+        j = p.partner[k];
+        kmax = p.sx[k].y;
+        kb = p.syz[k];
+        kv = p.sv[k];
+        kf = p.sflag[k];
+        acc = 0;
+        taken = 0;
+      }
+    }
+    qhead = (qhead + ntake) & (Q - 1);
+    qsize -= ntake;
+    __syncwarp();
+    const bool active = k >= 0;
+    if (__ballot_sync(kFullMask, active) == 0) {
+      if (!more && qsize == 0) break;
+      continue;
+    }
+    // 3. U candidates of the lane's run: the valid ones are the prefix before
+    //    the first x-test failure (a NaN sentinel ends every list).
+    float xm[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xm[u] = active ? p.sx[j + u].x : 0.f;
+    int nvalid = 0;
+    if (active) {
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+        if (nvalid == u && xm[u] <= kmax) ++nvalid;
+    }
+    tested += unsigned(nvalid);
+    bool hit[U];
+    int2 pr[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      hit[u] = false;
+      pr[u] = make_int2(0, 0);
+      if (u < nvalid) {
+        const float4 b = p.syz[j + u];
+        if (overlap_bc(kb, b)) {
+          const int4 bv = p.sv[j + u];
+          bool h = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
+          if (h && (kf & 3) != 3) h = ((kf | p.sflag[j + u]) & 3) == 3;
+          hit[u] = h;
+          pr[u] = make_int2(min(kv.w, bv.w), max(kv.w, bv.w));
+        }
+      }
+    }
+    // 4. Emit the step's hits through the warp's staging buffer.
+    int nh = 0;
+#pragma unroll
+    for (int u = 0; u < U; ++u) nh += hit[u] ? 1 : 0;
+    if (COUNT) {
+      acc += nh;
+    } else {
+      const unsigned anym = __ballot_sync(kFullMask, nh > 0);
+      if (anym) {
+        int total = 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const unsigned hm = __ballot_sync(kFullMask, hit[u]);
+          if (hit[u]) st[staged + __popc(hm & below)] = pr[u];
+          staged += __popc(hm);
+          total += __popc(hm);
+        }
+        // per-scene counts: one register while the warp stays in one scene
+        if (!multi) {
+          wpairs += unsigned(total);
+        } else {
+          const int lead = __shfl_sync(kFullMask, kf >> 2, __ffs(anym) - 1);
+          if (__all_sync(kFullMask, nh == 0 || (kf >> 2) == lead)) {
+            if (lead != wscene) {
+              if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+              wscene = lead;
+              wpairs = 0;
+            }
+            wpairs += unsigned(total);
+          } else if (nh) {
+            atomicAdd(&p.scene_pairs[kf >> 2], (unsigned long long)nh);
+          }
+        }
+        if (staged >= 32) {
+          __syncwarp();
+          flush_staged(st, staged, lane, p);
+          staged = 0;
+        }
+      }
+    }
+    // 5. A lane whose U candidates all passed continues; otherwise its run ended.
+    if (active) {
+      if (nvalid == U) {
+        j += U;
+        taken += U;
+        if (p.run_cap && taken >= p.run_cap) {  // a long run: the warp pass takes the rest
+          p.long_list[atomicAdd(p.long_items, 1u)] = make_int2(k, j);
+          if (COUNT) p.box_counts[k - p.begin] = acc;
+          k = -1;
+        }
+      } else {
+        if (COUNT) p.box_counts[k - p.begin] = acc;
+        k = -1;
+      }
+    }
+  }
+  if (!COUNT) {
+    __syncwarp();
+    if (staged) flush_staged(st, staged, lane, p);
+    if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+    const unsigned t = __reduce_add_sync(kFullMask, tested);
+    if (lane == 0 && p.stats) atomicAdd(p.stats, (unsigned long long)t);
+  }
+}
+
+// The warp pass over the runs the lane sweep handed over (runs longer than
+// SweepParams::run_cap, which would keep one lane or group busy long after the
+// others finished). One warp per run; each step tests 32 * U consecutive
+// candidates, lane l taking j + 32u + l; the valid ones are those before the
+// first x-test failure in position order (the padding after the last list
+// covers the reads past it). All pairs of a run belong to its start box's scene.
+template <int U, bool COUNT>
+__global__ void __launch_bounds__(256)
+stq_long_run_kernel(const SweepParams p) {
+  constexpr int STAGE = 32 * (U + 1);
+  __shared__ int2 stage[COUNT ? 1 : 8][COUNT ? 1 : STAGE];
+  const int lane = threadIdx.x & 31;
+  const unsigned below = lanemask_lt();
+  int2 *st = stage[COUNT ? 0 : (threadIdx.x >> 5)];
+  const unsigned n_items = *p.long_items;
+  if (n_items == 0) return;
+  int staged = 0;
+  unsigned tested = 0;
+  while (true) {
+    unsigned item = 0;
+    if (lane == 0) item = atomicAdd(p.long_work, 1u);
+    item = __shfl_sync(kFullMask, item, 0);
+    if (item >= n_items) break;
+    const int2 it = p.long_list[item];
+    const int k = it.x;
+    int j = it.y;
+    const float kmax = p.sx[k].y;
+    const float4 kb = p.syz[k];
+    const int4 kv = p.sv[k];
+    const int kf = p.sflag[k];
+    unsigned run_hits = 0;  // warp-uniform (emit) or this lane's (count mode)
+    while (true) {
+      float xm[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) xm[u] = p.sx[j + 32 * u + lane].x;
+      int first = 32 * U;  // offset of the first x-test failure
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const unsigned fm = __ballot_sync(kFullMask, !(xm[u] <= kmax));
+        if (first == 32 * U && fm) first = 32 * u + __ffs(fm) - 1;
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int off = 32 * u + lane;
+        bool hit = false;
+        int2 pr = make_int2(0, 0);
+        if (off < first) {
+          ++tested;
+          const float4 b = p.syz[j + off];
+          if (overlap_bc(kb, b)) {
+            const int4 bv = p.sv[j + off];
+            hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
+            if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j + off]) & 3) == 3;
+            pr = make_int2(min(kv.w, bv.w), max(kv.w, bv.w));
+          }
+        }
+        if (COUNT) {
+          run_hits += hit ? 1u : 0u;
+        } else {
+          const unsigned hm = __ballot_sync(kFullMask, hit);
+          if (hit) st[staged + __popc(hm & below)] = pr;
+          staged += __popc(hm);
+          run_hits += unsigned(__popc(hm));
+        }
+      }
+      if (!COUNT && staged >= 32) {
+        __syncwarp();
+        flush_staged(st, staged, lane, p);
+        staged = 0;
+      }
+      if (first < 32 * U) break;
+      j += 32 * U;
+    }
+    if (COUNT) {
+      const unsigned total = __reduce_add_sync(kFullMask, run_hits);
+      if (lane == 0 && total) atomicAdd(&p.box_counts[k - p.begin], int(total));
+    } else if (lane == 0 && run_hits) {
+      atomicAdd(&p.scene_pairs[kf >> 2], (unsigned long long)run_hits);
+    }
+  }
+  if (!COUNT) {
+    __syncwarp();
+    if (staged) flush_staged(st, staged, lane, p);
+    const unsigned t = __reduce_add_sync(kFullMask, tested);
+    if (lane == 0 && p.stats) atomicAdd(p.stats, (unsigned long long)t);
+  }
+}
+
+template <typename Kern>
+cudaError_t launch_persistent(Kern kern, int block, cudaStream_t s, const SweepParams &p, int num_sms) {
   int per_sm = 0;
-  auto kern = stq_sweep_kernel<G, Q, BLOCK, COUNT>;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, 0);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   // persistent grid: all resident blocks, capped by the available work
   const int64_t warps_needed = (int64_t(p.end - p.begin) + p.chunk - 1) / p.chunk;
   int64_t blocks = int64_t(num_sms) * per_sm;
-  const int64_t max_useful = (warps_needed + BLOCK / 32 - 1) / (BLOCK / 32);
+  const int64_t max_useful = (warps_needed + block / 32 - 1) / (block / 32);
   if (blocks > max_useful) blocks = max_useful;
   if (blocks < 1) blocks = 1;
-  kern<<<unsigned(blocks), BLOCK, 0, s>>>(p);
+  kern<<<unsigned(blocks), block, 0, s>>>(p);
   return cudaGetLastError();
 }
 
-template <int G, int Q, int BLOCK>
-cudaError_t launch_gqb(cudaStream_t s, const SweepParams &p, int sms) {
-  return launch_variant<G, Q, BLOCK, false>(s, p, sms);
+template <int G, int Q, int BLOCK, bool COUNT>
+cudaError_t launch_variant(cudaStream_t s, const SweepParams &p, int num_sms) {
+  return launch_persistent(stq_sweep_kernel<G, Q, BLOCK, COUNT>, BLOCK, s, p, num_sms);
 }
 
 template <int G, int Q>
 cudaError_t launch_gq(cudaStream_t s, const SweepParams &p, int block, int sms) {
   switch (block) {
-    case 128: return launch_gqb<G, Q, 128>(s, p, sms);
-    case 512: return launch_gqb<G, Q, 512>(s, p, sms);
-    default: return launch_gqb<G, Q, 256>(s, p, sms);
+    case 128: return launch_variant<G, Q, 128, false>(s, p, sms);
+    case 512: return launch_variant<G, Q, 512, false>(s, p, sms);
+    default: return launch_variant<G, Q, 256, false>(s, p, sms);
   }
 }
 
@@ -227,6 +505,24 @@ cudaError_t launch_g(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
     case 32: return launch_gq<G, 32>(s, p, t.block, sms);
     case 128: return launch_gq<G, 128>(s, p, t.block, sms);
     default: return launch_gq<G, 64>(s, p, t.block, sms);
+  }
+}
+
+template <int U, int Q>
+cudaError_t launch_uq(cudaStream_t s, const SweepParams &p, int block, int sms) {
+  switch (block) {
+    case 128: return launch_persistent(stq_sweep_lane_kernel<U, Q, 128, false>, 128, s, p, sms);
+    case 512: return launch_persistent(stq_sweep_lane_kernel<U, Q, 512, false>, 512, s, p, sms);
+    default: return launch_persistent(stq_sweep_lane_kernel<U, Q, 256, false>, 256, s, p, sms);
+  }
+}
+
+template <int U>
+cudaError_t launch_u(cudaStream_t s, const SweepParams &p, const SweepTuning &t, int sms) {
+  switch (t.queue) {
+    case 32: return launch_uq<U, 32>(s, p, t.block, sms);
+    case 128: return launch_uq<U, 128>(s, p, t.block, sms);
+    default: return launch_uq<U, 64>(s, p, t.block, sms);
   }
 }
 
@@ -338,13 +634,37 @@ __global__ void pairs_keys_kernel(stq_pair *pairs, int64_t n, unsigned long long
 
 }  // namespace
 
+static cudaError_t launch_long_runs(cudaStream_t s, const SweepParams &p, bool count_mode, int num_sms) {
+  if (!p.run_cap) return cudaSuccess;
+  if (count_mode) stq_long_run_kernel<4, true><<<unsigned(num_sms * 2), 256, 0, s>>>(p);
+  else stq_long_run_kernel<4, false><<<unsigned(num_sms * 2), 256, 0, s>>>(p);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_sweep_lanes(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
+                                      bool count_mode, int num_sms);
+
 cudaError_t launch_sweep(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
                          bool count_mode, int num_sms) {
   if (p.end <= p.begin) return cudaSuccess;
+  cudaError_t e = launch_sweep_lanes(s, p, t, count_mode, num_sms);
+  if (e != cudaSuccess) return e;
+  return launch_long_runs(s, p, count_mode, num_sms);
+}
+
+static cudaError_t launch_sweep_lanes(cudaStream_t s, const SweepParams &p, const SweepTuning &t,
+                                      bool count_mode, int num_sms) {
   if (count_mode)  // per-start-box counts do not depend on the tuning
     return launch_variant<8, 64, 256, true>(s, p, num_sms);
+  if (t.lanes == 1) {  // one start box per lane
+    switch (t.per_lane) {
+      case 1: return launch_u<1>(s, p, t, num_sms);
+      case 2: return launch_u<2>(s, p, t, num_sms);
+      case 8: return launch_u<8>(s, p, t, num_sms);
+      default: return launch_u<4>(s, p, t, num_sms);
+    }
+  }
   switch (t.lanes) {
-    case 1: return launch_g<1>(s, p, t, num_sms);
     case 2: return launch_g<2>(s, p, t, num_sms);
     case 4: return launch_g<4>(s, p, t, num_sms);
     case 16: return launch_g<16>(s, p, t, num_sms);

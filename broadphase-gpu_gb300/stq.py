@@ -42,7 +42,7 @@ STQ_ERR_NOT_PREPARED = -7
 
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
 OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
-OPT_REPLICA_BUDGET, OPT_GRAPH, OPT_HOST_OVERLAP = 7, 8, 9
+OPT_REPLICA_BUDGET, OPT_GRAPH, OPT_HOST_OVERLAP, OPT_PER_LANE, OPT_RUN_CAP = 7, 8, 9, 10, 11
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
@@ -98,6 +98,7 @@ ABI_SIGNATURES = {
                                          ctypes.POINTER(ctypes.c_int)]),
     "stq_server_mesh": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp]),
     "stq_server_stats": (ctypes.c_int, [_vp, _c_i64p, _c_i64p, _c_i64p, _c_i64p]),
+    "stq_server_set_option": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int64]),
     "stq_read_mesh": (ctypes.c_int, [ctypes.c_char_p, _vp, _c_i64p, _vp, _c_i64p]),
     "stq_mesh_edges": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _c_i64p]),
     "stq_compare_truth_json": (ctypes.c_int, [ctypes.c_char_p, _vp, ctypes.c_int64, _c_i64p, _c_i64p,
@@ -318,7 +319,7 @@ class Context:
         self._check(self.lib.stq_autotune(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1, _ptr(pairs),
                                           capacity, ctypes.byref(ms)))
         names = {OPT_LANES: "lanes", OPT_QUEUE: "queue", OPT_BLOCK: "block", OPT_RADIX_BITS: "radix_bits",
-                 OPT_CELL_SCALE: "cell_scale"}
+                 OPT_CELL_SCALE: "cell_scale", OPT_PER_LANE: "per_lane"}
         return ms.value, {v: self.get_option(k) for k, v in names.items()}
 
     def batch_scene_pairs(self, n_scenes: int) -> np.ndarray:
@@ -419,6 +420,11 @@ class Server:
         if st != STQ_OK:
             raise STQError(st, "request not active")
         return V0, V1
+
+    def set_option(self, option: int, value: int) -> None:
+        st = self.lib.stq_server_set_option(self._h, option, value)
+        if st != STQ_OK:
+            raise STQError(st, "server option")
 
     def stats(self) -> dict:
         a, q, b, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

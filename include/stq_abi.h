@@ -82,9 +82,10 @@ enum { STQ_AXIS_AUTO = -1, STQ_AXIS_X = 0, STQ_AXIS_Y = 1, STQ_AXIS_Z = 2 };
 
 /* Tuning knobs for stq_context_set_option (0 restores the automatic choice). */
 typedef enum stq_option {
-  STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1,2,4,8,16,32 */
-  STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 32, 64 or 128           */
-  STQ_OPT_BLOCK_SIZE = 3,      /* sweep block size: 128, 256 or 512               */
+  STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1 (default),
+                                  2, 4, 8, 16, 32                                   */
+  STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 32, 64 (default) or 128 */
+  STQ_OPT_BLOCK_SIZE = 3,      /* sweep block size: 128, 256 (default) or 512     */
   STQ_OPT_CELLS = 4,           /* cell grid on the two non-sweep axes: 0 automatic,
                                   1 no cells (plain sweep), k > 1 a k x k grid      */
   STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
@@ -94,10 +95,15 @@ typedef enum stq_option {
                                   default 4); finer grids beyond it are coarsened   */
   STQ_OPT_GRAPH = 8,           /* stq_batch_broadphase: 1 capture and replay a CUDA
                                   graph (default), 2 plain stream launches          */
-  STQ_OPT_HOST_OVERLAP = 9     /* stq_sweep_host / stq_broadphase_host: 1 sweep in
+  STQ_OPT_HOST_OVERLAP = 9,    /* stq_sweep_host / stq_broadphase_host: 1 sweep in
                                   windows, each window's pairs copied to the host
                                   while the next is swept (default), 2 one copy
                                   after the whole sweep                            */
+  STQ_OPT_CANDIDATES_PER_LANE = 10, /* with one lane per entry: candidates a lane
+                                  tests per step, 1, 2, 4 or 8 (default)        */
+  STQ_OPT_RUN_CAP = 11         /* candidates of one start box a lane (group) tests
+                                  before a whole warp takes over the rest of its
+                                  run (1..2^20, default 512)                      */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -292,6 +298,9 @@ int stq_server_mesh(stq_server *server, int64_t request_id, double *h_V0, double
 /* active, queued, bytes held for admitted requests, ticks launched */
 int stq_server_stats(stq_server *server, int64_t *active, int64_t *queued, int64_t *bytes,
                      int64_t *ticks);
+/* stq_context_set_option on the server's pipeline; the next tick captures
+ * its launch sequence again with the new setting. */
+int stq_server_set_option(stq_server *server, int option, int64_t value);
 
 /* ---- sweep without any allocation -----------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device

@@ -61,10 +61,12 @@ def test_batch_build_matches_single_builds(ctx, stq, oracle, cuda, scenes):
 
 
 @pytest.mark.parametrize("mixed_axes", [False, True])
-def test_batch_prepare_and_sweep(ctx, stq, oracle, cuda, scenes, mixed_axes):
+@pytest.mark.parametrize("run_cap", [0, 3])
+def test_batch_prepare_and_sweep(ctx, stq, oracle, cuda, scenes, mixed_axes, run_cap):
     import torch
 
     meshes, want = scenes
+    ctx.set_option(stq.OPT_RUN_CAP, run_cap)
     V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
     n = sum(m.num_boxes for m in meshes)
     boxes = torch.empty((n, 11), dtype=torch.int32, device=cuda)
@@ -166,7 +168,8 @@ def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes)
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
     ms, settings = ctx.autotune(boxes, bo, pairs, cap)
     assert ms > 0
-    assert settings["lanes"] in (4, 8, 16, 32) and settings["queue"] in (32, 64, 128)
+    assert settings["lanes"] in (1, 4, 8, 16) and settings["queue"] in (32, 64, 128)
+    assert settings["per_lane"] in (2, 4, 8) or settings["lanes"] > 1
     assert settings["block"] in (128, 256, 512) and settings["radix_bits"] in (4, 8)
     assert settings["cell_scale"] in (1, 2, 4)
     r = ctx.sweep_prepared(pairs, cap)

@@ -141,6 +141,73 @@ def test_sweep_tuning_space(ctx, stq, oracle, cuda, c0, lanes, queue, block):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("per_lane", [1, 2, 4, 8])
+@pytest.mark.parametrize("queue", [32, 128])
+@pytest.mark.parametrize("block", [128, 512])
+def test_sweep_one_lane_per_box(ctx, stq, oracle, cuda, c0, per_lane, queue, block):
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_LANES, 1)
+    ctx.set_option(stq.OPT_PER_LANE, per_lane)
+    ctx.set_option(stq.OPT_QUEUE, queue)
+    ctx.set_option(stq.OPT_BLOCK, block)
+    assert ctx.get_option(stq.OPT_PER_LANE) == per_lane
+    for axis in (0, -1):
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, want), axis
+
+
+@pytest.mark.parametrize("run_cap", [1, 5, 64])
+@pytest.mark.parametrize("shape", [(1, 4), (1, 8), (8, 0), (2, 0)])
+def test_long_runs_go_to_the_warp_pass(ctx, stq, oracle, cuda, c0, run_cap, shape):
+    """Runs longer than the cap continue in the warp pass: same pairs, same
+    candidates tested as without the hand-over."""
+    m, boxes, want = c0
+    ctx.set_option(stq.OPT_LANES, shape[0])
+    if shape[1]:
+        ctx.set_option(stq.OPT_PER_LANE, shape[1])
+    ctx.set_option(stq.OPT_RUN_CAP, (1 << 20))
+    sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
+    cand = ctx.candidates
+    ctx.set_option(stq.OPT_RUN_CAP, run_cap)
+    assert ctx.get_option(stq.OPT_RUN_CAP) == run_cap
+    got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
+    assert np.array_equal(got, want)
+    assert ctx.candidates == cand
+
+
+@pytest.fixture(scope="module")
+def dense_cloth(stq, oracle):
+    """Two cloth sheets 0.002 apart with large motion (sigma 0.03): coarse
+    cells, long lists and runs of thousands of candidates."""
+    m = stq.cloth_pair(g=90, z_offset=0.002, sigma=0.03, seed=9)
+    boxes = oracle.construct_boxes(m.V0, m.V1, m.E, m.F, stq.AABB_DTYPE)
+    return m, boxes, oracle.broadphase(boxes)
+
+
+@pytest.mark.parametrize("run_cap", [0, 16])
+def test_dense_scene_vs_oracle(ctx, stq, oracle, cuda, dense_cloth, run_cap):
+    import torch
+
+    m, boxes, want = dense_cloth
+    assert len(want) > 40 * len(boxes)
+    ctx.set_option(stq.OPT_RUN_CAP, run_cap)
+    got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1, cap=len(want) + 8)
+    assert np.array_equal(got, want)
+    # overflow and resume: count mode adds the warp pass's counts
+    cap = len(want) // 7 + 1
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    ctx.prepare(boxes_dev(boxes, cuda), len(boxes), -1)
+    start, chunks = 0, []
+    while start < ctx.prepared_length:
+        r = ctx.sweep_prepared(pairs, cap, start=start)
+        assert r.next_start > start
+        chunks.append(pairs[: r.count].cpu().numpy().copy())
+        start = r.next_start
+    assert len(chunks) >= 7
+    allp = np.concatenate(chunks)
+    assert np.array_equal(oracle.canonical(allp), want) and len(allp) == len(want)
+
+
 def test_sweep_radix_4bit(ctx, stq, oracle, cuda, c0):
     m, boxes, want = c0
     ctx.set_option(stq.OPT_RADIX_BITS, 4)
