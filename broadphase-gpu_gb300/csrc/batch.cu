@@ -81,31 +81,55 @@ __global__ void __launch_bounds__(kBlock)
 batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
                    SceneRecord *scenes, BatchHeader *hdr) {
   if (int(blockIdx.x) >= hdr->n_tiles) return;
+  constexpr int W = 11;  // words per box
+  __shared__ uint32_t stage[kBlock / 32][32 * W];
   const TileRec t = tiles[blockIdx.x];
-  double s1[3] = {0, 0, 0}, s2[3] = {0, 0, 0};
+  const int lane = threadIdx.x & 31;
+  uint32_t *sm = stage[threadIdx.x >> 5];
+  // moments about the tile's first box centre, in fp32 per thread (fp64 is
+  // slow on this part); the block combines them in fp64 and shifts them back
+  float c[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float m = 0.5f * (boxes[t.begin].min[k] + boxes[t.begin].max[k]);
+    c[k] = isfinite(m) ? m : 0.f;
+  }
+  float s1[3] = {0.f, 0.f, 0.f}, s2[3] = {0.f, 0.f, 0.f};
   uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   bool inverted = false, nan = false;
-  for (int i = threadIdx.x; i < t.count; i += kBlock) {
-    const stq_aabb &b = boxes[t.begin + i];
+  // warp-staged loads: 32 boxes as 11 coalesced word loads
+  const uint32_t *src = reinterpret_cast<const uint32_t *>(boxes + t.begin);
+  for (int i0 = threadIdx.x - lane; i0 < t.count; i0 += kBlock) {
+    const int n = min(32, t.count - i0);
+    for (int w = lane; w < n * W; w += 32) sm[w] = src[int64_t(i0) * W + w];
+    __syncwarp();
+    if (lane < n) {
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const float l = b.min[k], h = b.max[k];
-      nan |= (l != l) | (h != h);
-      inverted |= l > h;
-      s1[k] += double(l) + double(h);
-      s2[k] += double(l) * double(l) + double(h) * double(h);
-      lo[k] = min(lo[k], float_key(l));
-      hi[k] = max(hi[k], float_key(h));
+      for (int k = 0; k < 3; ++k) {
+        const float l = __uint_as_float(sm[lane * W + 1 + k]), h = __uint_as_float(sm[lane * W + 4 + k]);
+        nan |= (l != l) | (h != h);
+        inverted |= l > h;
+        const float dl = l - c[k], dh = h - c[k];
+        s1[k] += dl + dh;
+        s2[k] += dl * dl + dh * dh;
+        lo[k] = min(lo[k], float_key(l));
+        hi[k] = max(hi[k], float_key(h));
+      }
     }
+    __syncwarp();
   }
   __shared__ double dred[kBlock / 32];
   SceneRecord &r = scenes[t.scene];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    const double a = block_sum(s1[k], dred);
-    if (threadIdx.x == 0) atomicAdd(&r.s1[k], a);
-    const double c = block_sum(s2[k], dred);
-    if (threadIdx.x == 0) atomicAdd(&r.s2[k], c);
+    // sum(l + h) = S1 + 2 n c; sum(l^2 + h^2) = S2 + 2 c S1 + 2 n c^2
+    const double a = block_sum(double(s1[k]), dred);
+    const double q = block_sum(double(s2[k]), dred);
+    if (threadIdx.x == 0) {
+      const double ck = c[k], n = double(t.count);
+      atomicAdd(&r.s1[k], a + 2.0 * n * ck);
+      atomicAdd(&r.s2[k], q + 2.0 * ck * a + 2.0 * n * ck * ck);
+    }
     const uint32_t l = __reduce_min_sync(kFullMask, lo[k]);
     const uint32_t h = __reduce_max_sync(kFullMask, hi[k]);
     if ((threadIdx.x & 31) == 0) {

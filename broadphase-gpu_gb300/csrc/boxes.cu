@@ -12,27 +12,20 @@ namespace {
 
 constexpr int kBuildBlock = 256;
 
-// Min/max over the trajectory points of one primitive, per coordinate, in
-// fp64; the reference rounds that extreme to float, moves it one ulp outward
-// and widens it by nextafter_up(inflation_radius)
-// (src/aabb.cu:193-304; equal, by monotonicity of each step, to the CPU
-// builder's per-vertex rounding then union, src/cpu/aabb.cpp:23-95).
-__device__ __forceinline__ void finish_box(const double lo[3], const double hi[3],
-                                           float r_up, stq_aabb &b) {
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    b.min[k] = __fsub_rn(ref_next_down(__double2float_rn(lo[k])), r_up);
-    b.max[k] = __fadd_rn(ref_next_up(__double2float_rn(hi[k])), r_up);
-  }
+// Min/max over the trajectory points of one primitive, per coordinate; the
+// reference takes the extreme in fp64, rounds it to float, moves it one ulp
+// outward and widens it by nextafter_up(inflation_radius) (src/aabb.cu:193-304).
+// Rounding to float is monotone (overflow goes to +-inf, NaN stays NaN), so
+// rounding every point first and taking the extreme in float gives the same
+// bits (the CPU builder's order, src/cpu/aabb.cpp:23-95); it keeps the fp64
+// work to one conversion per coordinate, fp64 being slow on this part.
+__device__ __forceinline__ void load_point(const double *V, int64_t i, float p[3]) {
+  p[0] = __double2float_rn(V[3 * i]);
+  p[1] = __double2float_rn(V[3 * i + 1]);
+  p[2] = __double2float_rn(V[3 * i + 2]);
 }
 
-__device__ __forceinline__ void load_point(const double *V, int64_t i, double p[3]) {
-  p[0] = V[3 * i];
-  p[1] = V[3 * i + 1];
-  p[2] = V[3 * i + 2];
-}
-
-__device__ __forceinline__ void include_point(const double p[3], double lo[3], double hi[3]) {
+__device__ __forceinline__ void include_point(const float p[3], float lo[3], float hi[3]) {
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     lo[k] = p[k] < lo[k] ? p[k] : lo[k];
@@ -40,16 +33,16 @@ __device__ __forceinline__ void include_point(const double p[3], double lo[3], d
   }
 }
 
-// One output box t of a scene with nV vertices, nE edges, nF faces: boxes in
-// id order vertices, edges, faces (constructBoxes, src/io.cu:15-28);
-// vertexIds as src/aabb.cu:243, 210, 285.
-__device__ __forceinline__ void build_one(const double *__restrict__ V0,
-                                          const double *__restrict__ V1, int64_t nV,
-                                          const int32_t *__restrict__ E, int64_t nE,
-                                          const int32_t *__restrict__ F, int64_t t, int id,
-                                          float r_up, stq_aabb *__restrict__ out, int *flags) {
+// One box t of a scene with nV vertices, nE edges, nF faces: boxes in id
+// order vertices, edges, faces (constructBoxes, src/io.cu:15-28); vertexIds
+// as src/aabb.cu:243, 210, 285.
+__device__ __forceinline__ stq_aabb build_one(const double *__restrict__ V0,
+                                              const double *__restrict__ V1, int64_t nV,
+                                              const int32_t *__restrict__ E, int64_t nE,
+                                              const int32_t *__restrict__ F, int64_t t, int id,
+                                              float r_up, int *flags) {
   stq_aabb b;
-  double lo[3], hi[3], p[3];
+  float lo[3], hi[3], p[3];
   int idx[3];
   int npts;
   if (t < nV) {
@@ -86,8 +79,7 @@ __device__ __forceinline__ void build_one(const double *__restrict__ V0,
   if (!ok) {
     atomicOr(flags, kFlagBadIndex);
     for (int k = 0; k < 3; ++k) b.min[k] = b.max[k] = __int_as_float(0x7fc00000);
-    *out = b;
-    return;
+    return b;
   }
   load_point(V0, idx[0], p);
   for (int k = 0; k < 3; ++k) lo[k] = hi[k] = p[k];
@@ -99,8 +91,31 @@ __device__ __forceinline__ void build_one(const double *__restrict__ V0,
     load_point(V1, idx[q], p);
     include_point(p, lo, hi);
   }
-  finish_box(lo, hi, r_up, b);
-  *out = b;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    b.min[k] = __fsub_rn(ref_next_down(lo[k]), r_up);
+    b.max[k] = __fadd_rn(ref_next_up(hi[k]), r_up);
+  }
+  return b;
+}
+
+constexpr int kBoxWords = int(sizeof(stq_aabb) / 4);  // 11
+static_assert(sizeof(stq_aabb) == 44, "44-byte boxes");
+
+// The warp's boxes out[base, base + count), lane l holding box base + l, go
+// through shared memory and out as consecutive 4-byte words: 11 coalesced
+// stores per 32 boxes instead of 11 strided stores per box.
+__device__ __forceinline__ void store_boxes(const stq_aabb &b, bool have, int64_t base, int count,
+                                            stq_aabb *__restrict__ out, uint32_t *sm, int lane) {
+  if (have) {
+    const uint32_t *w = reinterpret_cast<const uint32_t *>(&b);
+#pragma unroll
+    for (int f = 0; f < kBoxWords; ++f) sm[lane * kBoxWords + f] = w[f];
+  }
+  __syncwarp();
+  uint32_t *dst = reinterpret_cast<uint32_t *>(out + base);
+  for (int i = lane; i < count * kBoxWords; i += 32) dst[i] = sm[i];
+  __syncwarp();
 }
 
 __global__ void __launch_bounds__(kBuildBlock)
@@ -108,10 +123,16 @@ build_boxes_kernel(const double *__restrict__ V0, const double *__restrict__ V1,
                    int64_t nV, const int32_t *__restrict__ E, int64_t nE,
                    const int32_t *__restrict__ F, int64_t nF, float r_up,
                    stq_aabb *__restrict__ out, int *flags) {
+  __shared__ uint32_t stage[kBuildBlock / 32][32 * kBoxWords];
+  const int lane = threadIdx.x & 31;
   const int64_t N = nV + nE + nF;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < N;
-       t += int64_t(gridDim.x) * blockDim.x)
-    build_one(V0, V1, nV, E, nE, F, t, int(t), r_up, out + t, flags);
+  const int64_t step = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) - lane; base < N; base += step) {
+    const int64_t t = base + lane;
+    stq_aabb b;
+    if (t < N) b = build_one(V0, V1, nV, E, nE, F, t, int(t), r_up, flags);
+    store_boxes(b, t < N, base, int(N - base < 32 ? N - base : 32), out, stage[threadIdx.x >> 5], lane);
+  }
 }
 
 // Batched: box t belongs to the scene s with box_off[s] <= t < box_off[s+1];
@@ -122,21 +143,30 @@ batch_build_kernel(const double *__restrict__ V0, const double *__restrict__ V1,
                    const long long *__restrict__ eoff, const int32_t *__restrict__ F,
                    const long long *__restrict__ foff, const long long *__restrict__ box_off,
                    BatchHeader *hdr, float r_up, stq_aabb *__restrict__ out) {
+  __shared__ uint32_t stage[kBuildBlock / 32][32 * kBoxWords];
+  const int lane = threadIdx.x & 31;
   const int n_scenes = hdr->n_scenes;
   const int64_t n_boxes = hdr->n_boxes;
   int *flags = &hdr->flags;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_boxes;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    int lo = 0, hi = n_scenes - 1;  // last scene with box_off[s] <= t
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (box_off[mid] <= t) lo = mid;
-      else hi = mid - 1;
+  const int64_t step = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) - lane; base < n_boxes;
+       base += step) {
+    const int64_t t = base + lane;
+    stq_aabb b;
+    if (t < n_boxes) {
+      int lo = 0, hi = n_scenes - 1;  // last scene with box_off[s] <= t
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (box_off[mid] <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      const int s = lo;
+      const int64_t v0 = voff[s], e0 = eoff[s], f0 = foff[s];
+      b = build_one(V0 + 3 * v0, V1 + 3 * v0, voff[s + 1] - v0, E + 2 * e0, eoff[s + 1] - e0,
+                    F + 3 * f0, t - box_off[s], int(t), r_up, flags);
     }
-    const int s = lo;
-    const int64_t v0 = voff[s], e0 = eoff[s], f0 = foff[s];
-    build_one(V0 + 3 * v0, V1 + 3 * v0, voff[s + 1] - v0, E + 2 * e0, eoff[s + 1] - e0,
-              F + 3 * f0, t - box_off[s], int(t), r_up, out + t, flags);
+    store_boxes(b, t < n_boxes, base, int(n_boxes - base < 32 ? n_boxes - base : 32), out, stage[threadIdx.x >> 5],
+                lane);
   }
 }
 
@@ -145,18 +175,27 @@ batch_build_kernel(const double *__restrict__ V0, const double *__restrict__ V1,
 __global__ void __launch_bounds__(kBuildBlock)
 batch_build_refs_kernel(const MeshRef *__restrict__ refs, const long long *__restrict__ box_off,
                         BatchHeader *hdr, float r_up, stq_aabb *__restrict__ out) {
+  __shared__ uint32_t stage[kBuildBlock / 32][32 * kBoxWords];
+  const int lane = threadIdx.x & 31;
   const int n_scenes = hdr->n_scenes;
   const int64_t n_boxes = hdr->n_boxes;
-  for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n_boxes;
-       t += int64_t(gridDim.x) * blockDim.x) {
-    int lo = 0, hi = n_scenes - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (box_off[mid] <= t) lo = mid;
-      else hi = mid - 1;
+  const int64_t step = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t base = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) - lane; base < n_boxes;
+       base += step) {
+    const int64_t t = base + lane;
+    stq_aabb b;
+    if (t < n_boxes) {
+      int lo = 0, hi = n_scenes - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (box_off[mid] <= t) lo = mid;
+        else hi = mid - 1;
+      }
+      const MeshRef &m = refs[lo];
+      b = build_one(m.V0, m.V1, m.nV, m.E, m.nE, m.F, t - box_off[lo], int(t), r_up, &hdr->flags);
     }
-    const MeshRef &m = refs[lo];
-    build_one(m.V0, m.V1, m.nV, m.E, m.nE, m.F, t - box_off[lo], int(t), r_up, out + t, &hdr->flags);
+    store_boxes(b, t < n_boxes, base, int(n_boxes - base < 32 ? n_boxes - base : 32), out, stage[threadIdx.x >> 5],
+                lane);
   }
 }
 
