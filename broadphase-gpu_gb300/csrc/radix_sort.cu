@@ -19,9 +19,11 @@ constexpr int kSortBlock = 256;
 constexpr int kSortWarps = kSortBlock / 32;
 
 template <typename K> struct TileShape {
-  static constexpr int items = sizeof(K) == 4 ? 16 : 8;
+  static constexpr int items = 8;  // 16 for 4-byte keys needs 89 registers: 2 blocks per SM
   static constexpr int tile = kSortBlock * items;
 };
+static_assert(TileShape<uint32_t>::tile == kRadixTile && TileShape<unsigned long long>::tile == kRadixTile,
+              "radix tile of the workspace sizing");
 
 int64_t num_tiles(int64_t n, int tile) { return (n + tile - 1) / tile; }
 

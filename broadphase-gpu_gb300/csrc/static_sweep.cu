@@ -26,7 +26,7 @@ constexpr size_t kOffKeys1 = kOffKeys0 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kOffVals0 = kOffKeys1 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kOffVals1 = kOffVals0 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kOffSortWs = kOffVals1 + up256(sizeof(uint32_t) * kMax);
-constexpr size_t kSortWsBytes = sizeof(uint32_t) * (256 * ((kMax + 4095) / 4096) + 256) + 256;
+constexpr size_t kSortWsBytes = sizeof(uint32_t) * (256 * ((kMax + kRadixTile - 1) / kRadixTile) + 256) + 256;
 constexpr size_t kOffSx = kOffSortWs + up256(kSortWsBytes);
 constexpr size_t kOffSyz = kOffSx + up256(sizeof(float2) * kSlots);
 constexpr size_t kOffSv = kOffSyz + up256(sizeof(float4) * kSlots);

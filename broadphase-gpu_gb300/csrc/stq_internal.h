@@ -263,6 +263,7 @@ cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long l
 // kbuf/vbuf are double buffers; *which receives the buffer index holding the
 // result. Returns workspace bytes when called with workspace == nullptr.
 size_t radix_workspace_bytes(int64_t n, int key_bytes, int bits);
+constexpr int kRadixTile = 2048;  // keys per radix tile (one per-digit count each)
 cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
                            int64_t n, int bits, void *workspace, int *which,
                            int64_t *launches, const unsigned int *d_n = nullptr);
