@@ -317,7 +317,7 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   ctx->scene.sflag = ctx->sflag.as<int>();
   ctx->scene.partner = ctx->partner.as<int>();
   stage_begin(ctx, kGather);
-  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene.sx, b.hdr, ctx->slot_cap),
+  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene, b.hdr, ctx->slot_cap),
            "launch sentinel fill");
   STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, r, b.cell_base, b.scenes,
                                     b.seg_count, b.seg_scan, ctx->scene),

@@ -468,12 +468,18 @@ list_max_kernel(const uint32_t *__restrict__ seg_count, BatchHeader *__restrict_
 }
 
 __global__ void __launch_bounds__(kBlock)
-fill_sentinels_kernel(float2 *__restrict__ sx, const BatchHeader *hdr, int64_t slots_cap) {
+fill_sentinels_kernel(float2 *__restrict__ sx, int *__restrict__ partner, const BatchHeader *hdr,
+                      int64_t slots_cap) {
   const int64_t slots = min(slots_cap, int64_t(hdr->length) + 1 + kSortedPad);
   const float q = __int_as_float(0x7fc00000);
+  // every position a sentinel until the gather writes the replicas: NaN
+  // bounds, and a partner that points at itself, so that the sweep's refill
+  // test of a sentinel position reads inside the scene (and fails)
   for (int64_t k = blockIdx.x * int64_t(kBlock) + threadIdx.x; k < slots;
-       k += int64_t(gridDim.x) * kBlock)
+       k += int64_t(gridDim.x) * kBlock) {
     sx[k] = make_float2(q, q);
+    partner[k] = int(k);
+  }
 }
 
 // Sorted replica p of segment s (cell c, type t; s = 3c + t) goes to
@@ -604,9 +610,9 @@ cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, 
   return cudaGetLastError();
 }
 
-cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, const BatchHeader *hdr,
+cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
                                   int64_t slots_cap) {
-  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(sx, hdr, slots_cap);
+  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(scene.sx, scene.partner, hdr, slots_cap);
   return cudaGetLastError();
 }
 

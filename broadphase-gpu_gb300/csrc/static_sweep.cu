@@ -87,6 +87,7 @@ __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, 
   } else if (k < n + 1 + kSortedPad) {
     const float q = __int_as_float(0x7fc00000);
     sx[k] = make_float2(q, q);
+    partner[k] = k;
   }
 }
 

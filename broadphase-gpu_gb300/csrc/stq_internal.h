@@ -225,7 +225,7 @@ cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b);
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n);
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms);
 
-cudaError_t launch_fill_sentinels(cudaStream_t s, float2 *sx, const BatchHeader *hdr,
+cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
                                   int64_t slots_cap);
 cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
