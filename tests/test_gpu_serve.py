@@ -39,6 +39,27 @@ def test_each_timestep_is_exact(stq, oracle, cuda):
     assert want[0][0] > 0 and len(set(w[1] for w in want)) == 4  # the scene moved
 
 
+@pytest.mark.parametrize("shape", [(1, 8), (4, 0), (8, 0)])
+def test_server_sweep_shapes_agree(stq, cuda, shape):
+    """stq_server_set_option retunes the server's sweep (the next tick captures
+    again); every shape gives the same per-step counts and checksums."""
+    mesh = stq.cloth_pair(g=60, z_offset=0.003, sigma=0.006, seed=8)
+    results = []
+    for s in ((8, 0), shape):
+        with stq.Server(0, None, budget_bytes=8 << 30, max_boxes=1 << 20, max_scenes=8) as sv:
+            sv.set_option(stq.OPT_LANES, s[0])
+            if s[1]:
+                sv.set_option(stq.OPT_PER_LANE, s[1])
+            sv.set_option(stq.OPT_RUN_CAP, 4)  # the warp pass too
+            rid = sv.submit(mesh, steps=3, sigma=0.003, seed=5)
+            run_until_done(sv, [rid])
+            results.append(sv.result(rid))
+    assert np.array_equal(results[0][0], results[1][0]) and np.array_equal(results[0][1], results[1][1])
+    with pytest.raises(stq.STQError):
+        with stq.Server(0, None, budget_bytes=8 << 30, max_boxes=1 << 20, max_scenes=8) as sv:
+            sv.set_option(stq.OPT_LANES, 3)
+
+
 def test_same_result_alone_and_in_a_mix(stq, cuda):
     target = stq.cloth_pair(g=30, z_offset=0.003, sigma=0.005, seed=41)
     others = [stq.cloth_pair(g=g, z_offset=0.004, sigma=0.004, seed=50 + g) for g in (12, 55, 20, 70, 33)]
