@@ -208,6 +208,105 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
             "batched_over_plain": t_plain / t_batch, "graph": True}
 
 
+def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush):
+    """64 scenes of 500,000 random boxes (95% small, lognormal extents around
+    0.002; 5% slivers stretched 200x along a random axis), sweep axis x in half
+    of the scenes and the largest-variance axis in the other half: the batched
+    prepare + sweep against a per-scene loop of the same calls."""
+    import numpy as np
+
+    n_s, per = 64, 500_000
+    scenes = [stq.random_boxes(per, sliver_frac=0.05, seed=1000 + k) for k in range(n_s)]
+    allb = np.concatenate(scenes)
+    allb["id"] = np.arange(len(allb), dtype=np.int32)
+    box_off = np.arange(n_s + 1, dtype=np.int64) * per
+    axes = [0 if k % 2 == 0 else stq.AXIS_AUTO for k in range(n_s)]
+    boxes = torch.from_numpy(allb.view(np.int32).reshape(-1, 11).copy()).to(dev)
+    ctx = stq.Context(local, stream.cuda_stream)
+    cap = 8 * len(allb)
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    ctx.batch_prepare(boxes, box_off, axes=axes)
+    total = ctx.sweep_prepared(pairs, cap).total
+    cap = int(total * 1.05) + 1024
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+
+    def timed(fn):
+        for _ in range(warmup):
+            fn()
+        ms = 0.0
+        for i in range(steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(i)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            ms += a.elapsed_time(b)
+        return ms / steps
+
+    def batched():
+        ctx.batch_prepare(boxes, box_off, axes=axes)
+        r = ctx.sweep_prepared(pairs, cap)
+        assert r.count == total
+
+    def plain_loop():
+        found = 0
+        for k in range(n_s):
+            ctx.prepare(boxes[k * per:(k + 1) * per], per, axes[k])
+            found += ctx.sweep_prepared(pairs, cap).count
+        assert found == total, (found, total)
+
+    t_batch = timed(batched)
+    t_plain = timed(plain_loop)
+    ctx.close()
+    n = len(allb)
+    return {"workload": "64 x 500k random boxes, 5% slivers (200x), axis x / max-variance alternating",
+            "boxes": n, "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain,
+            "batched_boxes_per_s": n / (t_batch / 1e3), "batched_pairs_per_s": total / (t_batch / 1e3),
+            "batched_over_plain": t_plain / t_batch}
+
+
+def bench_scene(stq, torch, dev, stream, local, steps, warmup, flush, workload):
+    """Device-resident step (build, prepare, sweep) on another single scene."""
+    mesh = make_mesh(stq, WORKLOADS[workload])
+    n = mesh.num_boxes
+    V0, V1, E, F = (torch.from_numpy(x).to(dev) for x in (mesh.V0, mesh.V1, mesh.E, mesh.F))
+    boxes = torch.empty((n, 11), dtype=torch.int32, device=dev)
+    ctx = stq.Context(local, stream.cuda_stream)
+    ctx.build_boxes(V0, V1, E, F, boxes)
+    ctx.prepare(boxes, n, stq.AXIS_AUTO)
+    cap = 24 * n
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    total = ctx.sweep_prepared(pairs, cap).total
+    cap = int(total * 1.05) + 1024
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    ctx.autotune(boxes, [0, n], pairs, cap)
+
+    def step():
+        ctx.build_boxes(V0, V1, E, F, boxes)
+        ctx.prepare(boxes, n, stq.AXIS_AUTO)
+        assert ctx.sweep_prepared(pairs, cap).count == total
+
+    for _ in range(warmup):
+        step()
+    ms = 0.0
+    for i in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(i)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        step()
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        ms += a.elapsed_time(b)
+    ms /= steps
+    ctx.close()
+    return {"workload": workload, "boxes": n, "pairs": int(total), "ms_per_step": ms,
+            "boxes_per_s": n / (ms / 1e3), "pairs_per_s": total / (ms / 1e3),
+            "pipeline_alg_frac": (60 * n + 8 * total) / (ms / 1e3) / 1e9 / measured_peak()[0]}
+
+
 def bench_serving(stq, local, n_requests, rate, seed=4):
     """Poisson arrivals of time-stepped cloth-pair requests (boxes log-uniform
     in [1e4, 2e6], 1-20 steps, step noise 0.003, HBM budget 160 GB): the
@@ -296,6 +395,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the 8M-box scene and the skewed 64-scene batch")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (use the library defaults), e.g. for profiling")
     ap.add_argument("--serve-requests", type=int, default=48)
@@ -468,6 +569,12 @@ def main():
 
     if not args.no_batch:
         line["batched"] = bench_batched(stq, torch, dev, stream, local, args.steps, args.warmup, flush)
+
+    if not args.no_extra:
+        if args.workload != "crumpled16x290":
+            line["scene_8m"] = bench_scene(stq, torch, dev, stream, local, args.steps, args.warmup, flush,
+                                           "crumpled16x290")
+        line["skewed"] = bench_skewed(stq, torch, dev, stream, local, args.steps, args.warmup, flush)
 
     if not args.no_serve and rank == 0:
         line["serve"] = bench_serving(stq, local, args.serve_requests, args.serve_rate)

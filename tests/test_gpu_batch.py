@@ -156,6 +156,32 @@ def test_batch_with_empty_and_tiny_scenes(ctx, stq, oracle, cuda):
     check_batch(oracle, pairs[: r.count].cpu().numpy(), bo, want, ctx.batch_scene_pairs(len(boxes)))
 
 
+def test_batch_skewed_boxes_mixed_axes(ctx, stq, oracle, cuda):
+    """Random boxes with 5% slivers stretched 200x, several scenes in one batch,
+    the sweep axis fixed to x in half of them and chosen by variance in the
+    others: each scene's pairs equal the oracle's on that scene alone."""
+    import torch
+
+    sizes = [30_000, 1, 12_000, 45_000, 0, 25_000]
+    boxes = [stq.random_boxes(n, sliver_frac=0.05, seed=70 + k) if n else np.zeros(0, stq.AABB_DTYPE)
+             for k, n in enumerate(sizes)]
+    bo = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    allb = np.concatenate(boxes)
+    allb["id"] = np.arange(len(allb))
+    want = []
+    for k in range(len(sizes)):
+        bb = allb[bo[k]:bo[k + 1]].copy()
+        want.append(oracle.broadphase(bb) - bo[k] if len(bb) else np.zeros((0, 2), np.int32))
+    d = torch.from_numpy(allb.view(np.int32).reshape(-1, 11).copy()).to(cuda)
+    axes = [0 if k % 2 == 0 else -1 for k in range(len(sizes))]
+    ctx.batch_prepare(d, bo, axes=axes)
+    cap = sum(len(w) for w in want) + 8
+    pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+    r = ctx.sweep_prepared(pairs, cap)
+    assert r.status == stq.STQ_OK
+    check_batch(oracle, pairs[: r.count].cpu().numpy(), bo, want, ctx.batch_scene_pairs(len(sizes)))
+
+
 def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes):
     import torch
 
