@@ -16,6 +16,10 @@
 // takes the next pending box, so a long run never stalls the other groups.
 // Refill, hand-out and pair output use __ballot_sync/__popc compaction: no
 // shared-memory atomics, and one global atomic per warp step that emits.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "stq_device.cuh"
 #include "stq_internal.h"
 
@@ -469,10 +473,33 @@ stq_long_run_kernel(const SweepParams p) {
   }
 }
 
+// Resident blocks per SM of a sweep kernel, queried once per kernel and
+// device: the query costs host time on every launch otherwise, and the host
+// calls launch one sweep per window back to back.
+template <typename Kern>
+cudaError_t resident_blocks(Kern kern, int block, int *per_sm) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, int> known;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const auto key = std::make_pair(reinterpret_cast<const void *>(kern), dev);
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = known.find(key);
+  if (it == known.end()) {
+    int v = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, block, 0);
+    if (e != cudaSuccess) return e;
+    it = known.emplace(key, v).first;
+  }
+  *per_sm = it->second;
+  return cudaSuccess;
+}
+
 template <typename Kern>
 cudaError_t launch_persistent(Kern kern, int block, cudaStream_t s, const SweepParams &p, int num_sms) {
   int per_sm = 0;
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, block, 0);
+  cudaError_t e = resident_blocks(kern, block, &per_sm);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) per_sm = 1;
   // persistent grid: all resident blocks, capped by the available work
