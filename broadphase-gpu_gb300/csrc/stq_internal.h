@@ -180,17 +180,6 @@ cudaError_t launch_build_boxes(cudaStream_t s, const double *V0, const double *V
                                int64_t nV, const int32_t *E, int64_t nE,
                                const int32_t *F, int64_t nF, float r_up,
                                stq_aabb *out, int *flags);
-// axis: partial sums then the final choice, written to *d_axis
-cudaError_t launch_axis_select(cudaStream_t s, const stq_aabb *boxes, int64_t n,
-                               double *partials, int nblocks, int *d_axis);
-int axis_partial_blocks(int64_t n);
-// keys/values for the sort; axis read from *d_axis
-cudaError_t launch_prep_keys(cudaStream_t s, const stq_aabb *boxes, int64_t n,
-                             const int *d_axis, uint32_t *keys, uint32_t *vals,
-                             int *flags);
-cudaError_t launch_gather(cudaStream_t s, const stq_aabb *boxes,
-                          const uint32_t *order, int64_t n, const int *d_axis,
-                          SortedScene scene);
 
 // ---- batch prepare (scene table) ---------------------------------------------------
 // Buffers sized by host capacities; actual sizes come from the BatchHeader.

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (oracle/stq_oracle.cpp). TEST INFRASTRUCTURE.
 
-Only the tests, the smoke check and the benchmark's CPU-baseline leg use this
-module, as the checker. Parity status: unpinned by reference golden vectors
+Only the tests, the smoke check and the benchmark's CPU-baseline and reference
+legs use this module, to check and time against. Parity status: unpinned by reference golden vectors
 (the reference ships none and its CPU library cannot be built here); pinned
 by the hand-derived known-answer cases under tests/golden/.
 """

@@ -2,8 +2,8 @@
 //
 // A plain C++17 + OpenMP restatement of the reference's CPU path
 // (Ahdhn/broadphase-gpu src/cpu/aabb.cpp and src/cpu/sweep.cpp), used only
-// as the checker by the tests, by the smoke check and by the bench's CPU
-// baseline leg. Nothing in the product links or calls it.
+// by the tests, the smoke check and the bench's CPU baseline and reference
+// legs, to check and time against. Nothing in the product links or calls it.
 //
 // Parity status: parity unpinned by reference golden vectors. The reference
 // ships no tests, no golden vectors and no fixtures, and its CPU library
