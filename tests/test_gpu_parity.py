@@ -312,6 +312,51 @@ def test_empty_and_tiny(ctx, stq, oracle, cuda):
     assert r.count == 0
 
 
+def degenerate_scenes(stq):
+    """Geometry the grid policy and the sweep must survive: point boxes
+    (zero extent, median extent 0), boxes flat on one plane, every box the
+    same, huge and tiny coordinates side by side, and one giant box among
+    small ones."""
+    rng = np.random.default_rng(9)
+    out = {}
+    b = stq.random_boxes(20_000, sliver_frac=0.0, seed=21)
+    b["max"] = b["min"]  # points: pairs only where points coincide
+    b["min"][::7] = b["min"][3]
+    b["max"][::7] = b["min"][3]
+    out["points"] = b
+    b = stq.random_boxes(20_000, sliver_frac=0.05, seed=22)
+    b["min"][:, 2] = 0.25
+    b["max"][:, 2] = 0.25
+    out["plane"] = b
+    b = stq.random_boxes(1_500, sliver_frac=0.0, seed=23)
+    b["min"][:] = (0.1, 0.2, 0.3)
+    b["max"][:] = (0.4, 0.5, 0.6)
+    out["identical"] = b
+    b = stq.random_boxes(20_000, sliver_frac=0.0, seed=24)
+    k = rng.choice(len(b), 300, replace=False)
+    b["min"][k] = b["min"][k] * np.float32(3e30)
+    b["max"][k] = b["min"][k] + np.float32(1e29)
+    b["min"][:50] = -np.float32(1e-30)
+    b["max"][:50] = np.float32(1e-30)
+    out["magnitudes"] = b
+    b = stq.random_boxes(20_000, sliver_frac=0.0, seed=25)
+    b["min"][7] = (-1.0, -1.0, -1.0)
+    b["max"][7] = (2.0, 2.0, 2.0)
+    out["giant"] = b
+    return out
+
+
+@pytest.mark.parametrize("name", ["points", "plane", "identical", "magnitudes", "giant"])
+def test_degenerate_geometry_vs_oracle(ctx, stq, oracle, cuda, name):
+    boxes = degenerate_scenes(stq)[name]
+    want = oracle.broadphase(boxes)
+    for cells, axis in ((0, -1), (0, 0), (0, 2), (16, -1)):
+        ctx.set_option(stq.OPT_CELLS, cells)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis,
+                          cap=len(want) + 16)
+        assert np.array_equal(got, want), (name, cells, axis)
+
+
 def test_nan_bound_rejected(ctx, stq, cuda):
     import torch
 
