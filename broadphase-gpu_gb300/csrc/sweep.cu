@@ -303,27 +303,23 @@ stq_sweep_lane_kernel(const SweepParams p) {
         if (nvalid == u && xm[u] <= kmax) ++nvalid;
     }
     tested += unsigned(nvalid);
-    bool hit[U];
-    int2 pr[U];
+    // hits as bits; a hit's id is loaded again on output (an L1 hit) rather
+    // than kept in registers for the whole step
+    unsigned hits = 0;
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-      hit[u] = false;
-      pr[u] = make_int2(0, 0);
       if (u < nvalid) {
         const float4 b = p.syz[j + u];
         if (overlap_bc(kb, b)) {
           const int4 bv = p.sv[j + u];
           bool h = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
           if (h && (kf & 3) != 3) h = ((kf | p.sflag[j + u]) & 3) == 3;
-          hit[u] = h;
-          pr[u] = make_int2(min(kv.w, bv.w), max(kv.w, bv.w));
+          if (h) hits |= 1u << u;
         }
       }
     }
     // 4. Emit the step's hits through the warp's staging buffer.
-    int nh = 0;
-#pragma unroll
-    for (int u = 0; u < U; ++u) nh += hit[u] ? 1 : 0;
+    const int nh = __popc(hits);
     if (COUNT) {
       acc += nh;
     } else {
@@ -332,8 +328,12 @@ stq_sweep_lane_kernel(const SweepParams p) {
         int total = 0;
 #pragma unroll
         for (int u = 0; u < U; ++u) {
-          const unsigned hm = __ballot_sync(kFullMask, hit[u]);
-          if (hit[u]) st[staged + __popc(hm & below)] = pr[u];
+          const bool hit = (hits >> u) & 1u;
+          const unsigned hm = __ballot_sync(kFullMask, hit);
+          if (hit) {
+            const int id = p.sv[j + u].w;
+            st[staged + __popc(hm & below)] = make_int2(min(kv.w, id), max(kv.w, id));
+          }
           staged += __popc(hm);
           total += __popc(hm);
         }
