@@ -136,6 +136,24 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(inside)}
 
 
+def max_over_ranks(dist, value: float, device) -> float:
+    """The largest of the ranks' values (a timing): every rank gets it. With one
+    process (dist None) the value itself."""
+    if dist is None:
+        return value
+    import torch
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: int, world: int, seconds_max: float) -> float:
+    """Whole-job throughput of replicas: every rank processed units_per_rank in
+    its own time; the job took the slowest rank's time."""
+    return world * units_per_rank / seconds_max
+
+
 def cpu_baseline(stq, orc, boxes, budget_s: float, threads: int = 0):
     """Oracle sort of all boxes + sweep of every stride-th start box, scaled to
     the full scene: boxes/s of the reference's CPU algorithm on this host."""
@@ -487,16 +505,12 @@ def main():
     if dist:
         dist.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(dist, sum(step_ms), dev)
     launches = ctx.launches - launches0
     stages = ctx.stage_times()
     ctx.enable_timing(False)
     ms_per_step = total_ms / args.steps
-    value = world * n / (ms_per_step / 1e3)
+    value = job_rate(n, world, ms_per_step / 1e3)
 
     # dominant kernel and its roofline (algorithmic bytes per launch / launch time)
     dom = max(stages.items(), key=lambda kv: kv[1][0])
@@ -555,12 +569,8 @@ def main():
             ctx.broadphase_host(hmesh, hpairs, stq.AXIS_AUTO)
             ts_staged.append(time.perf_counter() - t0)
         ctx.set_option(stq.OPT_HOST_OVERLAP, 0)
-        e2e_s = sum(ts) / len(ts)
-        if dist:
-            t = torch.tensor([e2e_s], device=dev)
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            e2e_s = float(t.item())
-        line["e2e"] = {"value": world * n / e2e_s, "unit": "boxes/s",
+        e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
+        line["e2e"] = {"value": job_rate(n, world, e2e_s), "unit": "boxes/s",
                        "h2d_bytes_per_step": 48 * nV + 8 * nE + 12 * nF,
                        "d2h_bytes_per_step": 8 * er.count, "ms_per_step": e2e_s * 1e3,
                        "call": "stq_broadphase_host",

@@ -1,0 +1,50 @@
+"""bench.py's multi-GPU reporting, on CPU: replicas of the single-scene step,
+one per rank, report the slowest rank's time and the whole job's units over
+it (no data-path collective). Two gloo ranks on 127.0.0.1."""
+import os
+import sys
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def _rank(rank, world, port, times, out):
+    sys.path.insert(0, str(ROOT))
+    import torch.distributed as dist
+
+    import bench
+
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    t = bench.max_over_ranks(dist, times[rank], "cpu")
+    dist.barrier()
+    dist.destroy_process_group()
+    out.put((rank, t, bench.job_rate(1000, world, t)))
+
+
+def test_two_ranks_report_the_slowest_time_and_the_job_rate():
+    import torch.multiprocessing as mp
+
+    ctx = mp.get_context("spawn")
+    out = ctx.Queue()
+    port = 29500 + os.getpid() % 1000
+    times = [0.25, 0.5]
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, times, out)) for r in range(2)]
+    for p in procs:
+        p.start()
+    got = sorted(out.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    assert [g[1] for g in got] == [0.5, 0.5]      # every rank sees the max
+    assert [g[2] for g in got] == [4000.0, 4000.0]  # 2 ranks x 1000 units / 0.5 s
+
+
+def test_single_process_passes_values_through():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.max_over_ranks(None, 1.5, "cpu") == 1.5
+    assert bench.job_rate(10, 1, 2.0) == 5.0
