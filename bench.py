@@ -546,9 +546,10 @@ def main():
     }
 
     if not args.no_e2e:
-        pin = lambda a: torch.from_numpy(a).pin_memory().numpy()  # noqa: E731
-        hmesh = stq.Mesh(pin(mesh.V0), pin(mesh.V1), pin(mesh.E), pin(mesh.F))
-        hpairs = torch.empty((cap, 2), dtype=torch.int32).pin_memory().numpy()
+        hmesh_t = [torch.from_numpy(a).pin_memory() for a in (mesh.V0, mesh.V1, mesh.E, mesh.F)]
+        hmesh = stq.Mesh(*(t.numpy() for t in hmesh_t))
+        hpairs_t = torch.empty((cap, 2), dtype=torch.int32).pin_memory()
+        hpairs = hpairs_t.numpy()
         # the same (tuned) context, now through the host-memory call
         for _ in range(args.warmup):
             ctx.broadphase_host(hmesh, hpairs, stq.AXIS_AUTO)
@@ -569,13 +570,29 @@ def main():
             ctx.broadphase_host(hmesh, hpairs, stq.AXIS_AUTO)
             ts_staged.append(time.perf_counter() - t0)
         ctx.set_option(stq.OPT_HOST_OVERLAP, 0)
+
+        def link_ms(copy):  # the host link alone: the step's bytes, no compute
+            lt = []
+            for _ in range(args.warmup + args.steps):
+                torch.cuda.synchronize(dev)
+                t0 = time.perf_counter()
+                with torch.cuda.stream(stream):
+                    copy()
+                stream.synchronize()
+                lt.append(time.perf_counter() - t0)
+            return 1e3 * float(np.median(lt[args.warmup:]))
+
+        h2d_ms = link_ms(lambda: [d.copy_(h, non_blocking=True) for d, h in zip((V0, V1, E, F), hmesh_t)])
+        d2h_ms = link_ms(lambda: hpairs_t[:npairs].copy_(pairs[:npairs], non_blocking=True))
         e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
         line["e2e"] = {"value": job_rate(n, world, e2e_s), "unit": "boxes/s",
                        "h2d_bytes_per_step": 48 * nV + 8 * nE + 12 * nF,
                        "d2h_bytes_per_step": 8 * er.count, "ms_per_step": e2e_s * 1e3,
                        "call": "stq_broadphase_host",
-                       "pairs_out": "sweep windows, each copied while the next is swept",
-                       "one_copy_after_sweep_ms_per_step": 1e3 * sum(ts_staged) / len(ts_staged)}
+                       "pairs_out": "sweep windows, each copied while later ones are swept",
+                       "one_copy_after_sweep_ms_per_step": 1e3 * sum(ts_staged) / len(ts_staged),
+                       "link_alone_ms": {"h2d_mesh": h2d_ms, "d2h_pairs": d2h_ms,
+                                         "d2h_gbs": 8 * npairs / d2h_ms / 1e6}}
 
     if not args.no_batch:
         line["batched"] = bench_batched(stq, torch, dev, stream, local, args.steps, args.warmup, flush)

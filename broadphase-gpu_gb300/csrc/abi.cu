@@ -355,13 +355,11 @@ int prepare_exact(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *box_
   return STQ_OK;
 }
 
-static_assert(offsetof(BatchHeader, long_items) == offsetof(BatchHeader, work) + sizeof(int) &&
-                  offsetof(BatchHeader, long_work) == offsetof(BatchHeader, work) + 2 * sizeof(int),
-              "the sweep cursors are cleared as one block");
-
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
-              long long capacity, bool count_mode, bool reset, bool timed) {
+              long long capacity, bool count_mode, bool timed, const SweepCursors *cursors,
+              cudaStream_t stream) {
   BatchHeader *hdr = dev_hdr(ctx);
+  cudaStream_t s = cursors && stream ? stream : ctx->stream;
   SweepParams p;
   p.sx = ctx->scene.sx;
   p.syz = ctx->scene.syz;
@@ -388,16 +386,18 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.long_list = ctx->long_list.as<int2>();
   p.long_items = &hdr->long_items;
   p.long_work = &hdr->long_work;
-  if (reset) {
+  if (cursors) {
+    p.count = cursors->count;
+    p.work = cursors->work;
+    p.long_list = cursors->long_list;
+    p.long_items = cursors->long_items;
+    p.long_work = cursors->long_work;
+  } else {
     STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, hdr, p.scene_pairs, ctx->scene_cap), "reset sweep");
     ctx->launches += 1;
-  } else {
-    // work cursor and the warp pass's list and cursor (adjacent in the header)
-    STQ_CUDA(ctx, cudaMemsetAsync(&hdr->work, 0, sizeof(int) + 2 * sizeof(unsigned int), ctx->stream),
-             "restart work cursors");
   }
   if (timed) stage_begin(ctx, count_mode ? kCountSweep : kSweep);
-  STQ_CUDA(ctx, launch_sweep(ctx->stream, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
+  STQ_CUDA(ctx, launch_sweep(s, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
   if (timed) stage_end(ctx, count_mode ? kCountSweep : kSweep);
   ctx->launches += 1;
   return STQ_OK;
@@ -465,7 +465,8 @@ void stq_context_destroy(stq_context *ctx) {
                       &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
-                      &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux})
+                      &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux,
+                      &ctx->window_pairs, &ctx->window_long_list, &ctx->window_cursors})
       b->release();
     if (ctx->in_host) cudaFreeHost(ctx->in_host);
     if (ctx->h_hdr) cudaFreeHost(ctx->h_hdr);
@@ -474,7 +475,12 @@ void stq_context_destroy(stq_context *ctx) {
       cudaStreamSynchronize(ctx->copy_stream);
       cudaStreamDestroy(ctx->copy_stream);
     }
+    if (ctx->window_stream) {
+      cudaStreamSynchronize(ctx->window_stream);
+      cudaStreamDestroy(ctx->window_stream);
+    }
     if (ctx->h_window_pairs) cudaFreeHost(ctx->h_window_pairs);
+    if (ctx->window_start) cudaEventDestroy(ctx->window_start);
     for (cudaEvent_t e : ctx->window_done)
       if (e) cudaEventDestroy(e);
     for (int st = 0; st < kStages; ++st)
@@ -491,7 +497,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 11 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 12 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -529,6 +535,10 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
     case STQ_OPT_RUN_CAP:
       if (value > (int64_t(1) << 20)) return fail(ctx, STQ_ERR_INVALID_ARG, "run cap: 1..2^20");
       break;
+    case STQ_OPT_HOST_WINDOWS:
+      if (value == 1 || value > stq_context::kCopyWindows)
+        return fail(ctx, STQ_ERR_INVALID_ARG, "host windows: 2..32");
+      break;
     default:
       break;
   }
@@ -538,7 +548,7 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 11) return -1;
+  if (!ctx || option < 1 || option > 12) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
@@ -550,6 +560,7 @@ int64_t stq_context_get_option(const stq_context *ctx, int option) {
     case STQ_OPT_HOST_OVERLAP: return ctx->options[STQ_OPT_HOST_OVERLAP] == 2 ? 2 : 1;
     case STQ_OPT_CANDIDATES_PER_LANE: return ctx->tuning.per_lane;
     case STQ_OPT_RUN_CAP: return ctx->tuning.run_cap;
+    case STQ_OPT_HOST_WINDOWS: return ctx->options[STQ_OPT_HOST_WINDOWS] ? ctx->options[STQ_OPT_HOST_WINDOWS] : 16;
     default: return ctx->options[option];
   }
 }
@@ -883,80 +894,117 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
 namespace {
 
 // Sweeps the prepared scene into h_pairs. The start positions are cut into
-// up to kCopyWindows windows swept one after another on the context's stream;
-// the pair counter runs on across windows, so window i's pairs are the range
-// [count after i-1, count after i) of one device buffer. Once a window's
-// event fires, the host reads its counter and queues the copy of that range
-// on a second stream: the copy engine moves window i to the host while the
-// SMs sweep window i+1, and the pair list's device-to-host transfer (the
-// largest cost of a host-buffer call) overlaps the sweep instead of
-// following it. An overflow (more pairs than capacity) falls back to the
-// prefix rule of stq_sweep_prepared and one copy.
+// windows (STQ_OPT_HOST_WINDOWS, default 16) that alternate between two
+// slots: even windows sweep on the context's stream into e2e_pairs, odd
+// windows on a second stream into window_pairs. A slot's pair counter runs on
+// across its windows, so window w's pairs are the range of its slot's buffer
+// between the counts after windows w - 2 and w; after each window a one-thread
+// kernel stores the count in mapped host memory and restarts the slot's work
+// cursor and long-run list. Both streams are filled at once, so one
+// window's last blocks share the SMs with the next window's first instead of
+// leaving them idle. Once window w has finished, the host reads its count and
+// queues the copy of its range to the end of h_pairs filled so far on a third
+// stream: the pair list's device-to-host transfer, the largest cost of a
+// host-buffer call, runs beside the sweep instead of after it. If the pairs do
+// not fit h_pairs the call falls back to the prefix rule of
+// stq_sweep_prepared and one copy.
 int sweep_to_host(stq_context *ctx, stq_pair *h_pairs, int64_t capacity, int64_t *count,
                   int64_t *total) {
-  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1)),
-           "allocate pair staging");
+  const size_t pair_bytes = sizeof(stq_pair) * size_t(capacity > 0 ? capacity : 1);
+  STQ_CUDA(ctx, ctx->e2e_pairs.ensure(pair_bytes), "allocate pair staging");
   stq_pair *d_pairs = ctx->e2e_pairs.as<stq_pair>();
   const int64_t length = ctx->length;
   constexpr int64_t kMinWindow = int64_t(1) << 19;  // start positions
-  const int windows = int(std::min<int64_t>(stq_context::kCopyWindows, length / kMinWindow));
-  auto copy_all = [&](int64_t c) -> int {
-    if (c <= 0) return STQ_OK;
-    STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, d_pairs, sizeof(stq_pair) * size_t(c), cudaMemcpyDeviceToHost,
-                                  ctx->stream),
-             "copy pairs to host");
-    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
-    return STQ_OK;
-  };
-  if (windows < 2 || capacity == 0 || ctx->options[STQ_OPT_HOST_OVERLAP] == 2) {
+  const int64_t want = ctx->options[STQ_OPT_HOST_WINDOWS] ? ctx->options[STQ_OPT_HOST_WINDOWS] : 16;
+  const int windows = int(std::min<int64_t>(want, length / kMinWindow));
+  auto one_copy = [&]() -> int {
     int64_t next = 0;
     const int st = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, count, &next, total);
     if (st != STQ_OK && st != STQ_OVERFLOW) return st;
-    STQ_TRY(copy_all(*count));
+    if (*count > 0) {
+      STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs, d_pairs, sizeof(stq_pair) * size_t(*count),
+                                    cudaMemcpyDeviceToHost, ctx->stream),
+               "copy pairs to host");
+      STQ_CUDA(ctx, cudaStreamSynchronize(ctx->stream), "synchronise stream");
+    }
     return st;
-  }
-  if (!ctx->copy_stream)
-    STQ_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking), "create copy stream");
-  if (!ctx->h_window_pairs)
-    STQ_CUDA(ctx, cudaMallocHost(&ctx->h_window_pairs, sizeof(unsigned long long) * stq_context::kCopyWindows),
+  };
+  if (windows < 2 || capacity == 0 || ctx->options[STQ_OPT_HOST_OVERLAP] == 2) return one_copy();
+
+  STQ_CUDA(ctx, ctx->window_pairs.ensure(pair_bytes), "allocate pair staging");
+  STQ_CUDA(ctx, ctx->window_long_list.ensure(sizeof(int2) * size_t(ctx->slot_cap)), "allocate long-run list");
+  STQ_CUDA(ctx, ctx->window_cursors.ensure(2 * sizeof(WindowCounters)), "allocate window cursors");
+  for (cudaStream_t *st : {&ctx->copy_stream, &ctx->window_stream})
+    if (!*st) STQ_CUDA(ctx, cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "create stream");
+  if (!ctx->h_window_pairs) {
+    STQ_CUDA(ctx, cudaHostAlloc(&ctx->h_window_pairs, sizeof(unsigned long long) * stq_context::kCopyWindows,
+                                cudaHostAllocMapped),
              "allocate window counters");
-  for (int w = 0; w < windows; ++w)
+    STQ_CUDA(ctx, cudaHostGetDevicePointer(&ctx->d_window_pairs, ctx->h_window_pairs, 0),
+             "map window counters");
+  }
+  for (cudaEvent_t *e : {&ctx->window_start, &ctx->window_done[0]})
+    if (!*e) STQ_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "create event");
+  for (int w = 1; w < windows; ++w)
     if (!ctx->window_done[w])
       STQ_CUDA(ctx, cudaEventCreateWithFlags(&ctx->window_done[w], cudaEventDisableTiming), "create event");
-  BatchHeader *hdr = dev_hdr(ctx);
+
+  WindowCounters *wc = ctx->window_cursors.as<WindowCounters>();
+  stq_pair *slot_pairs[2] = {d_pairs, ctx->window_pairs.as<stq_pair>()};
+  int2 *slot_list[2] = {ctx->long_list.as<int2>(), ctx->window_long_list.as<int2>()};
+  cudaStream_t slot_stream[2] = {ctx->stream, ctx->window_stream};
+
+  // the header reset (candidate statistics) and the stage timer run on the
+  // context's stream; the second stream starts after them
+  STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, dev_hdr(ctx), ctx->scene_pairs.as<unsigned long long>(),
+                                   ctx->scene_cap),
+           "reset sweep");
+  ctx->launches += 1;
+  STQ_CUDA(ctx, cudaMemsetAsync(wc, 0, 2 * sizeof(WindowCounters), ctx->stream), "clear window cursors");
   stage_begin(ctx, kSweep);
+  STQ_CUDA(ctx, cudaEventRecord(ctx->window_start, ctx->stream), "record window start");
+  STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->window_stream, ctx->window_start, 0), "order window stream");
   for (int w = 0; w < windows; ++w) {
+    const int slot = w & 1;
+    cudaStream_t s = slot_stream[slot];
+    const SweepCursors cur{&wc[slot].pairs, &wc[slot].work, slot_list[slot], &wc[slot].long_items,
+                           &wc[slot].long_work};
     const int64_t b = length * w / windows, e = length * (w + 1) / windows;
-    STQ_TRY(run_sweep(ctx, b, e, d_pairs, capacity, false, w == 0, false));
-    STQ_CUDA(ctx, cudaMemcpyAsync(&ctx->h_window_pairs[w], &hdr->pairs, sizeof(unsigned long long),
-                                  cudaMemcpyDeviceToHost, ctx->stream),
-             "read window counter");
-    STQ_CUDA(ctx, cudaEventRecord(ctx->window_done[w], ctx->stream), "record window");
+    STQ_TRY(run_sweep(ctx, b, e, slot_pairs[slot], capacity, false, false, &cur, s));
+    // the count to the host by a kernel store: a copy here would wait behind
+    // the pair copies on the copy engines and hold up this stream's next window
+    STQ_CUDA(ctx, launch_window_step(s, &wc[slot], ctx->d_window_pairs + w), "publish window count");
+    ctx->launches += 1;
+    STQ_CUDA(ctx, cudaEventRecord(ctx->window_done[w], s), "record window");
   }
+  // the stage (and the header read below) ends when both streams have
+  for (int w = windows - 2; w < windows; ++w)
+    STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->window_done[w], 0), "join window streams");
   stage_end(ctx, kSweep);
   int64_t done = 0;
   for (int w = 0; w < windows; ++w) {
     STQ_CUDA(ctx, cudaEventSynchronize(ctx->window_done[w]), "wait for sweep window");
-    const int64_t c = std::min<int64_t>(int64_t(ctx->h_window_pairs[w]), capacity);
-    if (c > done)
-      STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs + done, d_pairs + done, sizeof(stq_pair) * size_t(c - done),
+    const volatile unsigned long long *hc = ctx->h_window_pairs;
+    const int64_t from = w >= 2 ? int64_t(hc[w - 2]) : 0;
+    const int64_t c = int64_t(hc[w]) - from;
+    if (c > capacity - done) {
+      // overflow: let the windows in flight end, then take the prefix rule
+      for (cudaStream_t st : {ctx->window_stream, ctx->stream, ctx->copy_stream})
+        STQ_CUDA(ctx, cudaStreamSynchronize(st), "synchronise window streams");
+      return one_copy();
+    }
+    if (c > 0)
+      STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs + done, slot_pairs[w & 1] + from, sizeof(stq_pair) * size_t(c),
                                     cudaMemcpyDeviceToHost, ctx->copy_stream),
                "copy window pairs to host");
-    done = std::max(done, c);
+    done += c;
   }
   STQ_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream), "synchronise copy stream");
-  STQ_TRY(read_header(ctx));
-  const int64_t found = int64_t(ctx->h_hdr->pairs);
-  if (total) *total = found;
-  if (found <= capacity) {
-    *count = found;
-    return STQ_OK;
-  }
-  int64_t next = 0;
-  const int st = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, count, &next, total);
-  if (st != STQ_OK && st != STQ_OVERFLOW) return st;
-  STQ_TRY(copy_all(*count));
-  return st;
+  STQ_TRY(read_header(ctx));  // waits for both streams (joined above); input flags
+  ctx->h_hdr->pairs = (unsigned long long)done;
+  if (total) *total = done;
+  *count = done;
+  return STQ_OK;
 }
 
 }  // namespace

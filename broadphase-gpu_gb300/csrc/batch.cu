@@ -569,7 +569,25 @@ reset_sweep_kernel(BatchHeader *hdr, unsigned long long *scene_pairs) {
   }
 }
 
+// After a window of a host-buffer sweep: stores the slot's running pair count
+// in page-locked host memory (a kernel store, so that no copy-engine work sits
+// between two windows of a stream while the engines move pair lists) and
+// restarts the slot's cursors for its next window.
+__global__ void window_step_kernel(WindowCounters *wc, unsigned long long *host_count) {
+  if (threadIdx.x != 0) return;
+  *reinterpret_cast<volatile unsigned long long *>(host_count) = wc->pairs;
+  wc->work = 0;
+  wc->long_items = 0u;
+  wc->long_work = 0u;
+  __threadfence_system();
+}
+
 }  // namespace
+
+cudaError_t launch_window_step(cudaStream_t s, WindowCounters *wc, unsigned long long *host_count) {
+  window_step_kernel<<<1, 32, 0, s>>>(wc, host_count);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long long *scene_pairs,
                                int scene_cap) {

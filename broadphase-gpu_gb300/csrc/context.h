@@ -100,12 +100,16 @@ struct stq_context {
   GraphKey graph_key;
   bool capturing = false;
 
-  // host-buffer calls: copy stream, one event and one pinned pair counter per
-  // sweep window
-  static constexpr int kCopyWindows = 8;
-  cudaStream_t copy_stream = nullptr;
+  // host-buffer calls: windows alternate between two sweep streams, each with
+  // its own pair buffer, counters and long-run list (slot 0 is the context's
+  // stream, e2e_pairs and long_list); a third stream copies pairs to the host
+  static constexpr int kCopyWindows = 32;
+  cudaStream_t copy_stream = nullptr, window_stream = nullptr;
+  cudaEvent_t window_start = nullptr;
   cudaEvent_t window_done[kCopyWindows] = {};
-  unsigned long long *h_window_pairs = nullptr;
+  unsigned long long *h_window_pairs = nullptr;  // page-locked, mapped
+  unsigned long long *d_window_pairs = nullptr;  // its device address
+  DevBuf window_pairs, window_long_list, window_cursors;
 
   // autotuner cache: shape bucket -> options (lanes, queue, block, radix, scale)
   std::vector<std::pair<int64_t, std::vector<int64_t>>> tuned;
@@ -153,12 +157,15 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_box
 // then the sorted scene. replicas: the replica count, or -1 (device count).
 int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, int64_t n_boxes,
                          int64_t replicas);
-// reset: clear the pair counter, per-scene counts and statistics first (a
-// window of a longer sweep keeps them and only restarts the work cursor).
-// timed: record the launch as one sweep stage (a windowed caller times all
-// its windows as one).
+// Launches one sweep over start positions [begin, end). With cursors null it
+// first clears the batch header's pair counter, cursors, per-scene counts and
+// statistics and uses them and the context's long-run list; otherwise it uses
+// the given counters (cleared by the caller on the launch stream) and
+// launches on stream, keeping the header's statistics. timed: record the
+// launch as one sweep stage (a windowed caller times its windows as one).
 int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs, long long capacity,
-              bool count_mode, bool reset = true, bool timed = true);
+              bool count_mode, bool timed = true,
+              const SweepCursors *cursors = nullptr, cudaStream_t stream = nullptr);
 
 template <typename T>
 T *dev_at(stq_context *ctx, size_t off) {

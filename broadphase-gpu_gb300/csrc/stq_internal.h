@@ -149,6 +149,25 @@ struct SortedScene {
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
 
+// Counters of one sweep launch that runs beside another (a host call's
+// windows alternate between two of these), in device memory.
+struct WindowCounters {
+  unsigned long long pairs;  // pairs found
+  int work;                  // grab cursor
+  unsigned int long_items;   // runs handed to the warp pass
+  unsigned int long_work;    // warp pass grab cursor
+  int pad;
+};
+
+// Where one sweep launch keeps its counters and handed-over runs.
+struct SweepCursors {
+  unsigned long long *count;
+  int *work;
+  int2 *long_list;
+  unsigned int *long_items;
+  unsigned int *long_work;
+};
+
 struct SweepParams {
   const float2 *sx;
   const float4 *syz;
@@ -247,6 +266,8 @@ cudaError_t launch_pair_checksums(cudaStream_t s, const stq_pair *pairs, long lo
                                   unsigned long long *checks, int scene_cap);
 cudaError_t launch_reset_sweep(cudaStream_t s, BatchHeader *hdr, unsigned long long *scene_pairs,
                                int scene_cap);
+// host_count: device address of page-locked, mapped host memory
+cudaError_t launch_window_step(cudaStream_t s, WindowCounters *wc, unsigned long long *host_count);
 
 // LSD radix sort of (uint32 key, uint32 value) or (uint64 key) pairs.
 // kbuf/vbuf are double buffers; *which receives the buffer index holding the

@@ -43,6 +43,7 @@ STQ_ERR_NOT_PREPARED = -7
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
 OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
 OPT_REPLICA_BUDGET, OPT_GRAPH, OPT_HOST_OVERLAP, OPT_PER_LANE, OPT_RUN_CAP = 7, 8, 9, 10, 11
+OPT_HOST_WINDOWS = 12
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p

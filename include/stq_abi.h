@@ -101,9 +101,12 @@ typedef enum stq_option {
                                   after the whole sweep                            */
   STQ_OPT_CANDIDATES_PER_LANE = 10, /* with one lane per entry: candidates a lane
                                   tests per step, 1, 2, 4 or 8 (default)        */
-  STQ_OPT_RUN_CAP = 11         /* candidates of one start box a lane (group) tests
+  STQ_OPT_RUN_CAP = 11,        /* candidates of one start box a lane (group) tests
                                   before a whole warp takes over the rest of its
                                   run (1..2^20, default 512)                      */
+  STQ_OPT_HOST_WINDOWS = 12    /* stq_sweep_host / stq_broadphase_host: windows a
+                                  sweep is cut into (2..32, default 16; fewer when
+                                  the scene has under 2^19 positions per window) */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -176,9 +179,9 @@ int stq_sweep(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int axis,
  * start boxes, copies the pairs back to h_pairs (capacity entries). Same
  * return codes as stq_sweep; on STQ_OVERFLOW h_pairs holds the prefix.
  * Scenes of 2^20 or more sweep positions are swept in windows of start
- * positions; each window's pairs are copied to h_pairs on a second stream
- * while the next window is swept (STQ_OPT_HOST_OVERLAP = 2: one copy after the
- * sweep). A page-locked h_pairs (cudaHostAlloc / cudaHostRegister) lets those
+ * positions, two at a time on two streams; each window's pairs are copied to
+ * h_pairs on a third stream while later windows are swept
+ * (STQ_OPT_HOST_OVERLAP = 2: one copy after the sweep). A page-locked h_pairs (cudaHostAlloc / cudaHostRegister) lets those
  * copies run asynchronously. The same holds for stq_broadphase_host. */
 int stq_sweep_host(stq_context *ctx, const stq_aabb *h_boxes, int64_t n,
                    int axis, stq_pair *h_pairs, int64_t capacity,

@@ -433,9 +433,9 @@ def big_cloth(stq):
 @pytest.mark.parametrize("overlap", [1, 2])
 @pytest.mark.parametrize("pinned", [True, False])
 def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, overlap, pinned):
-    """Host calls sweep large scenes in windows whose pair ranges are copied
-    while the next window runs (OPT_HOST_OVERLAP=1) or copy once after the
-    sweep (=2); both give the device sweep's pairs, into page-locked or
+    """Host calls sweep large scenes in windows, two at a time, each window's
+    pairs copied while later ones run (OPT_HOST_OVERLAP=1), or copy once after
+    the sweep (=2); both give the device sweep's pairs, into page-locked or
     pageable buffers, and the overflow prefix of the one-window path."""
     import torch
 
@@ -471,8 +471,10 @@ def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, over
         ctx.broadphase_host(m, out, stq.AXIS_AUTO)
         other = ctx.launches - l0
         ctx.set_option(stq.OPT_HOST_OVERLAP, overlap)
-        windows = min(8, length >> 19)
-        assert launches - other == (windows - 1 if overlap == 1 else 1 - windows)
+        windows = min(ctx.get_option(stq.OPT_HOST_WINDOWS), length >> 19)
+        assert windows == min(16, length >> 19)
+        # per window: a sweep and the kernel that publishes its pair count
+        assert launches - other == (2 * windows - 1 if overlap == 1 else 1 - 2 * windows)
         hb = boxes.cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
         r = ctx.sweep_host(hb, out)
         assert r.status == stq.STQ_OK and np.array_equal(oracle.canonical(out[: r.count]), want)
@@ -483,6 +485,47 @@ def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, over
         assert rs.status == ref.status == stq.STQ_OVERFLOW and rs.total == len(want)
         assert rs.count == ref.count
         assert np.array_equal(oracle.canonical(small[: rs.count]), oracle.canonical(dp[: ref.count].cpu().numpy()))
+
+
+@pytest.mark.parametrize("windows", [2, 3, 32])
+def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows):
+    """Any window count (odd counts end on the first slot; 32 is more than
+    this scene's 2^19-position windows allow) gives the device sweep's pairs;
+    a capacity that the first window alone exceeds gives the prefix rule's."""
+    import torch
+
+    m = big_cloth
+    with stq.Context(0) as ctx:
+        d = [torch.from_numpy(np.ascontiguousarray(x)).to(cuda) for x in (m.V0, m.V1, m.E, m.F)]
+        boxes = torch.empty((m.num_boxes, 11), dtype=torch.int32, device=cuda)
+        ctx.build_boxes(*d, boxes)
+        ctx.prepare(boxes, m.num_boxes, stq.AXIS_AUTO)
+        length = ctx.prepared_length
+        cap = 64 * m.num_boxes
+        dp = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
+        r = ctx.sweep_prepared(dp, cap)
+        want = oracle.canonical(dp[: r.count].cpu().numpy())
+        ctx.set_option(stq.OPT_HOST_WINDOWS, windows)
+        assert ctx.get_option(stq.OPT_HOST_WINDOWS) == windows
+        out = torch.empty((len(want), 2), dtype=torch.int32).pin_memory().numpy()
+        ctx.set_option(stq.OPT_HOST_OVERLAP, 2)
+        l0 = ctx.launches
+        ctx.broadphase_host(m, out, stq.AXIS_AUTO)
+        one = ctx.launches - l0
+        ctx.set_option(stq.OPT_HOST_OVERLAP, 1)
+        out[:] = -7
+        l0 = ctx.launches
+        r = ctx.broadphase_host(m, out, stq.AXIS_AUTO)
+        assert ctx.launches - l0 - one == 2 * min(windows, length >> 19) - 1
+        assert r.status == stq.STQ_OK and r.count == len(want)
+        assert np.array_equal(oracle.canonical(out), want)
+        tiny = np.empty((100, 2), np.int32)
+        hb = boxes.cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
+        rs = ctx.sweep_host(hb, tiny)
+        ref = ctx.sweep_prepared(dp, 100)
+        assert rs.status == ref.status == stq.STQ_OVERFLOW and rs.total == len(want)
+        assert rs.count == ref.count
+        assert np.array_equal(oracle.canonical(tiny[: rs.count]), oracle.canonical(dp[: ref.count].cpu().numpy()))
 
 
 def test_prepared_scene_reused_across_windows(ctx, stq, oracle, cuda, c0):
