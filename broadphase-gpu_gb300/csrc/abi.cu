@@ -244,7 +244,9 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
   STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->sfloor.ensure(sizeof(float2) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->partner.ensure(sizeof(int) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->cell_floor.ensure(sizeof(float2) * size_t(segs / 3 + 1)), "allocate cell bounds");
   STQ_CUDA(ctx, ctx->long_list.ensure(sizeof(int2) * slots), "allocate long-run list");
   ctx->rep_cap = int64_t(r);
   ctx->slot_cap = int64_t(slots);
@@ -315,15 +317,17 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   ctx->scene.syz = ctx->syz.as<float4>();
   ctx->scene.sv = ctx->sv.as<int4>();
   ctx->scene.sflag = ctx->sflag.as<int>();
+  ctx->scene.sfloor = ctx->sfloor.as<float2>();
   ctx->scene.partner = ctx->partner.as<int>();
   stage_begin(ctx, kGather);
   STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene, b.hdr, ctx->slot_cap),
            "launch sentinel fill");
   STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, r, b.cell_base, b.scenes,
-                                    b.seg_count, b.seg_scan, ctx->scene),
+                                    b.seg_count, b.seg_scan, ctx->cell_floor.as<float2>(), ctx->seg_cap / 3,
+                                    ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
-  ctx->launches += 4;
+  ctx->launches += 5;
   return STQ_OK;
 }
 
@@ -377,6 +381,7 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.work = &hdr->work;
   p.box_counts = ctx->box_counts.as<int32_t>();
   p.sflag = ctx->scene.sflag;
+  p.sfloor = ctx->scene.sfloor;
   p.partner = ctx->scene.partner;
   p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
   p.hdr = hdr;
@@ -461,7 +466,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
-                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->partner, &ctx->long_list,
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
                       &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],

@@ -482,6 +482,29 @@ fill_sentinels_kernel(float2 *__restrict__ sx, int *__restrict__ partner, const 
   }
 }
 
+// Lower bounds of every cell on the two non-sweep axes (-inf for the first
+// row or column, where no box can start below the cell).
+__global__ void __launch_bounds__(kBlock)
+cell_floor_kernel(const unsigned int *__restrict__ cell_base, const SceneRecord *__restrict__ scenes,
+                  const BatchHeader *hdr, float2 *__restrict__ cell_floor, long long cells_cap) {
+  // more cells than the buffers hold is the replica overflow: nothing is swept
+  const unsigned int cells = (long long)hdr->cells <= cells_cap ? hdr->cells : 0u;
+  const int S = hdr->n_scenes;
+  for (unsigned int cell = blockIdx.x * kBlock + threadIdx.x; cell < cells; cell += gridDim.x * kBlock) {
+    int lo = 0, hi = S - 1;  // scene of the cell
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (cell_base[mid] <= cell) lo = mid;
+      else hi = mid - 1;
+    }
+    const GridParams g = scenes[lo].grid;
+    const int local = int(cell - cell_base[lo]);
+    const int cb = local / g.nc, cc = local - cb * g.nc;
+    cell_floor[cell] = make_float2(cb > 0 ? cell_lower_bound(cb, g.ob, g.ib) : -INFINITY,
+                                   cc > 0 ? cell_lower_bound(cc, g.oc, g.ic) : -INFINITY);
+  }
+}
+
 // Sorted replica p of segment s (cell c, type t; s = 3c + t) goes to
 // position p + s: every list is followed by one NaN slot, which ends every
 // run at its list (and cell, and scene) boundary.
@@ -491,6 +514,10 @@ fill_sentinels_kernel(float2 *__restrict__ sx, int *__restrict__ partner, const 
 // two minima on b, on c) is the max of the two boxes' first cells; both boxes
 // lie in this cell, so the reference point is here exactly when, on each of
 // b and c, one of the two replicas is its box's first cell.
+// sfloor of a position: on b and on c, -inf if the cell is the box's first
+// cell there, else the cell's lower bound; a candidate is in its first cell
+// on an axis exactly when its minimum there is >= that bound, so the sweep
+// tests the rule on the candidate's bounds, which it loads anyway.
 // partner of a position: its first candidate. An edge's candidates are the
 // edges after it in its list; a vertex's are the cell's faces whose min is
 // >= its min (lower bound), a face's the cell's vertices whose min is > its
@@ -503,7 +530,8 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
                     const unsigned int *__restrict__ cell_base,
                     const SceneRecord *__restrict__ scenes, const uint32_t *__restrict__ seg_count,
                     const uint32_t *__restrict__ seg_scan, float2 *__restrict__ sx,
-                    float4 *__restrict__ syz, int4 *__restrict__ sv, int *__restrict__ sflag,
+                    const float2 *__restrict__ cell_floor, float4 *__restrict__ syz,
+                    int4 *__restrict__ sv, int *__restrict__ sflag, float2 *__restrict__ sfloor,
                     int *__restrict__ partner) {
   const int64_t R = hdr->replicas;
   const int S = hdr->n_scenes;
@@ -546,6 +574,13 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
     syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
     sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
     sflag[k] = (lo << 2) | (fc << 1) | fb;
+    float2 fl = make_float2(-INFINITY, -INFINITY);
+    if (!(fb && fc)) {
+      const float2 cf = cell_floor[cell];
+      if (!fb) fl.x = cf.x;
+      if (!fc) fl.y = cf.y;
+    }
+    sfloor[k] = fl;
     partner[k] = int(first);
   }
 }
@@ -639,11 +674,12 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
                                 const uint32_t *seg_count, const uint32_t *seg_scan,
-                                SortedScene scene) {
+                                float2 *cell_floor, int64_t cells_cap, SortedScene scene) {
+  cell_floor_kernel<<<blocks_for(cells_cap), kBlock, 0, s>>>(cell_base, scenes, hdr, cell_floor, cells_cap);
   gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
                                                              scenes, seg_count, seg_scan, scene.sx,
-                                                             scene.syz, scene.sv, scene.sflag,
-                                                             scene.partner);
+                                                             cell_floor, scene.syz, scene.sv,
+                                                             scene.sflag, scene.sfloor, scene.partner);
   return cudaGetLastError();
 }
 

@@ -31,7 +31,8 @@ constexpr size_t kOffSx = kOffSortWs + up256(kSortWsBytes);
 constexpr size_t kOffSyz = kOffSx + up256(sizeof(float2) * kSlots);
 constexpr size_t kOffSv = kOffSyz + up256(sizeof(float4) * kSlots);
 constexpr size_t kOffFlag = kOffSv + up256(sizeof(int4) * kSlots);
-constexpr size_t kOffPartner = kOffFlag + up256(sizeof(int) * kSlots);
+constexpr size_t kOffFloor = kOffFlag + up256(sizeof(int) * kSlots);
+constexpr size_t kOffPartner = kOffFloor + up256(sizeof(float2) * kSlots);
 constexpr size_t kOffHdr = kOffPartner + up256(sizeof(int) * kSlots);
 constexpr size_t kOffScenePairs = kOffHdr + up256(sizeof(BatchHeader));
 constexpr size_t kScratchBytes = kOffScenePairs + up256(sizeof(unsigned long long));
@@ -74,6 +75,7 @@ __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, 
   float4 *syz = reinterpret_cast<float4 *>(scratch + kOffSyz);
   int4 *sv = reinterpret_cast<int4 *>(scratch + kOffSv);
   int *sflag = reinterpret_cast<int *>(scratch + kOffFlag);
+  float2 *sfloor = reinterpret_cast<float2 *>(scratch + kOffFloor);
   int *partner = reinterpret_cast<int *>(scratch + kOffPartner);
   const int b = axis == 0 ? 1 : 0, c = axis == 2 ? 1 : 2;
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -83,6 +85,7 @@ __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, 
     syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
     sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
     sflag[k] = 3;  // one cell: every box is in its first cell on both axes
+    sfloor[k] = make_float2(-INFINITY, -INFINITY);
     partner[k] = k + 1;  // one list: candidates follow in sort order
   } else if (k < n + 1 + kSortedPad) {
     const float q = __int_as_float(0x7fc00000);
@@ -138,6 +141,7 @@ extern "C" int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, st
   p.syz = reinterpret_cast<const float4 *>(scratch + kOffSyz);
   p.sv = reinterpret_cast<const int4 *>(scratch + kOffSv);
   p.sflag = reinterpret_cast<const int *>(scratch + kOffFlag);
+  p.sfloor = reinterpret_cast<const float2 *>(scratch + kOffFloor);
   p.partner = reinterpret_cast<const int *>(scratch + kOffPartner);
   p.begin = 0;
   p.end = ni;

@@ -82,6 +82,31 @@ __device__ __forceinline__ int cell_coord(float v, float origin, float inv, int 
   return int(t);
 }
 
+// Lower bound of cell C (1 <= C <= n - 1) on one axis: the smallest float v
+// with cell_coord(v, origin, inv, n) >= C, i.e. with (v - origin) * inv >= C
+// in the same round-to-nearest steps. That test is monotone in v, so a binary
+// search over the floats in order (ordered bit patterns from -inf to +inf,
+// -0 just below +0; no NaN lies between) finds v exactly in 32 steps. For a
+// box of a replica in cell C, "C is the cell of the box's minimum" is then
+// "minimum >= the lower bound of C": the cell of the minimum is at most C.
+__device__ __forceinline__ float cell_lower_bound(int C, float origin, float inv) {
+  auto ordered = [](float f) {
+    const uint32_t u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  };
+  auto from_ordered = [](uint32_t k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+  };
+  const float fc = float(C);
+  uint32_t lo = ordered(-INFINITY), hi = ordered(INFINITY);  // test fails at lo, holds at hi
+  while (hi - lo > 1u) {
+    const uint32_t mid = lo + ((hi - lo) >> 1);
+    if (__fmul_rn(__fsub_rn(from_ordered(mid), origin), inv) >= fc) hi = mid;
+    else lo = mid;
+  }
+  return from_ordered(hi);
+}
+
 // ---- box type and pair filter ------------------------------------------------
 // Type from the signs of vertexIds (src/aabb.cu:12-31): vertex {v,-v-1,-v-1}
 // -> 0, edge {e0,e1,-e0-1} -> 1, face {f0,f1,f2} -> 2.

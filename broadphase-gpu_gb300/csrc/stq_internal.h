@@ -145,6 +145,8 @@ struct SortedScene {
   float4 *syz = nullptr;  // (min_b, min_c, max_b, max_c) on the other axes
   int4 *sv = nullptr;     // (vertexIds[0..2], id)
   int *sflag = nullptr;   // first-cell bits (0: along b, 1: along c), scene << 2
+  float2 *sfloor = nullptr;  // per axis b, c: -inf where the cell is the box's
+                             // first, else the cell's lower bound
   int *partner = nullptr; // first candidate position of each start position
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
@@ -180,6 +182,8 @@ struct SweepParams {
   int *work;
   int32_t *box_counts;       // count mode: pairs per start position (k - begin)
   const int *sflag;          // first-cell bits and scene of each position
+  const float2 *sfloor;      // first-cell rule of a start position on b and c:
+                             // a candidate passes if its minima are >= these
   const int *partner;        // first candidate position of each start position
   unsigned long long *scene_pairs;  // per-scene pair counters
   const BatchHeader *hdr;    // device sizes (length bounds the sweep range)
@@ -240,7 +244,7 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
                                 const uint32_t *seg_count, const uint32_t *seg_scan,
-                                SortedScene scene);
+                                float2 *cell_floor, int64_t cells_cap, SortedScene scene);
 // Batched box build: scene s has vertices [voff[s], voff[s+1]) etc.; box ids
 // are global (box_off[s] + local), vertex ids local to the scene.
 cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V1,

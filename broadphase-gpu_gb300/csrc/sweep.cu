@@ -66,9 +66,10 @@ stq_sweep_kernel(const SweepParams p) {
   float kmax = 0.f;
   float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
   int4 kv = make_int4(0, 0, 0, 0);
+  float2 kfl = make_float2(0.f, 0.f);  // first-cell rule of the current start box
   const int end = min(p.end, int(p.hdr->length));
   const int span = end - p.begin;
-  int kf = 0;  // first-cell bits and scene of the current start box
+  int kf = 0;  // scene of the current start box (above the first-cell bits)
   unsigned tested = 0;  // candidates this lane tested (statistics)
   // warp-uniform: staged pairs, and pairs of the current scene not yet added
   // to its counter
@@ -114,9 +115,10 @@ stq_sweep_kernel(const SweepParams p) {
         kmax = p.sx[k].y;
         kb = p.syz[k];
         kv = p.sv[k];
+        kfl = p.sfloor[k];
         acc = 0;
         taken = 0;
-        kf = p.sflag[k];
+        kf = multi ? p.sflag[k] : 0;
       }
     }
     qhead = (qhead + ntake) & (Q - 1);
@@ -138,13 +140,12 @@ stq_sweep_kernel(const SweepParams p) {
     if (valid) {
       ++tested;
       const float4 b = p.syz[j];
-      if (overlap_bc(kb, b)) {  // ids only for candidates that overlap on b and c
-        const int4 bv = p.sv[j];
-        hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
       // a pair found in several cells is emitted only in the cell of its
       // reference point: on b and on c, one of the two replicas must be its
-      // box's first cell (the candidate's bits are read only when needed)
-        if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j]) & 3) == 3;
+      // box's first cell (the candidate's: minimum >= the cell's lower bound)
+      if (overlap_bc(kb, b) && b.x >= kfl.x && b.y >= kfl.y) {  // ids only for these
+        const int4 bv = p.sv[j];
+        hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
         lo_id = min(kv.w, bv.w);
         hi_id = max(kv.w, bv.w);
       }
@@ -235,6 +236,7 @@ stq_sweep_lane_kernel(const SweepParams p) {
   float kmax = 0.f;
   float4 kb = make_float4(0.f, 0.f, 0.f, 0.f);
   int4 kv = make_int4(0, 0, 0, 0);
+  float2 kfl = make_float2(0.f, 0.f);  // first-cell rule of the start box
   const int end = min(p.end, int(p.hdr->length));
   const int span = end - p.begin;
   unsigned tested = 0;
@@ -278,7 +280,8 @@ stq_sweep_lane_kernel(const SweepParams p) {
         kmax = p.sx[k].y;
         kb = p.syz[k];
         kv = p.sv[k];
-        kf = p.sflag[k];
+        kfl = p.sfloor[k];
+        kf = multi ? p.sflag[k] : 0;
         acc = 0;
         taken = 0;
       }
@@ -310,11 +313,9 @@ stq_sweep_lane_kernel(const SweepParams p) {
     for (int u = 0; u < U; ++u) {
       if (u < nvalid) {
         const float4 b = p.syz[j + u];
-        if (overlap_bc(kb, b)) {
+        if (overlap_bc(kb, b) && b.x >= kfl.x && b.y >= kfl.y) {  // and the first-cell rule
           const int4 bv = p.sv[j + u];
-          bool h = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
-          if (h && (kf & 3) != 3) h = ((kf | p.sflag[j + u]) & 3) == 3;
-          if (h) hits |= 1u << u;
+          if ((p.typed || valid_pair(kv, bv)) && !covertex(kv, bv)) hits |= 1u << u;
         }
       }
     }
@@ -414,6 +415,7 @@ stq_long_run_kernel(const SweepParams p) {
     const float kmax = p.sx[k].y;
     const float4 kb = p.syz[k];
     const int4 kv = p.sv[k];
+    const float2 kfl = p.sfloor[k];
     const int kf = p.sflag[k];
     unsigned run_hits = 0;  // warp-uniform (emit) or this lane's (count mode)
     while (true) {
@@ -434,10 +436,9 @@ stq_long_run_kernel(const SweepParams p) {
         if (off < first) {
           ++tested;
           const float4 b = p.syz[j + off];
-          if (overlap_bc(kb, b)) {
+          if (overlap_bc(kb, b) && b.x >= kfl.x && b.y >= kfl.y) {  // and the first-cell rule
             const int4 bv = p.sv[j + off];
             hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
-            if (hit && (kf & 3) != 3) hit = ((kf | p.sflag[j + off]) & 3) == 3;
             pr = make_int2(min(kv.w, bv.w), max(kv.w, bv.w));
           }
         }
