@@ -240,7 +240,8 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
   STQ_CUDA(ctx, ctx->seg_scan_ws.ensure(scan_workspace_bytes(segs) + 16), "allocate segment scan");
   ctx->seg_cap = segs;
   const size_t slots = r + size_t(segs) + 1 + kSortedPad;
-  STQ_CUDA(ctx, ctx->sx.ensure(sizeof(float2) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->xmin.ensure(sizeof(float) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->xmax.ensure(sizeof(float) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->syz.ensure(sizeof(float4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sv.ensure(sizeof(int4) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
@@ -313,7 +314,8 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
                                     &which, &ctx->launches, &b.hdr->replicas, rbits),
            "launch list sort");
   stage_end(ctx, kSort);
-  ctx->scene.sx = ctx->sx.as<float2>();
+  ctx->scene.xmin = ctx->xmin.as<float>();
+  ctx->scene.xmax = ctx->xmax.as<float>();
   ctx->scene.syz = ctx->syz.as<float4>();
   ctx->scene.sv = ctx->sv.as<int4>();
   ctx->scene.sflag = ctx->sflag.as<int>();
@@ -365,7 +367,8 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   BatchHeader *hdr = dev_hdr(ctx);
   cudaStream_t s = cursors && stream ? stream : ctx->stream;
   SweepParams p;
-  p.sx = ctx->scene.sx;
+  p.xmin = ctx->scene.xmin;
+  p.xmax = ctx->scene.xmax;
   p.syz = ctx->scene.syz;
   p.sv = ctx->scene.sv;
   p.begin = int32_t(begin);
@@ -466,7 +469,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
-                      &ctx->vals[1], &ctx->sort_ws, &ctx->sx, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
                       &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],

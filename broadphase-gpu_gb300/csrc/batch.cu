@@ -468,7 +468,8 @@ list_max_kernel(const uint32_t *__restrict__ seg_count, BatchHeader *__restrict_
 }
 
 __global__ void __launch_bounds__(kBlock)
-fill_sentinels_kernel(float2 *__restrict__ sx, int *__restrict__ partner, const BatchHeader *hdr,
+fill_sentinels_kernel(float *__restrict__ xmin, float *__restrict__ xmax, int *__restrict__ partner,
+                      const BatchHeader *hdr,
                       int64_t slots_cap) {
   const int64_t slots = min(slots_cap, int64_t(hdr->length) + 1 + kSortedPad);
   const float q = __int_as_float(0x7fc00000);
@@ -477,7 +478,8 @@ fill_sentinels_kernel(float2 *__restrict__ sx, int *__restrict__ partner, const 
   // test of a sentinel position reads inside the scene (and fails)
   for (int64_t k = blockIdx.x * int64_t(kBlock) + threadIdx.x; k < slots;
        k += int64_t(gridDim.x) * kBlock) {
-    sx[k] = make_float2(q, q);
+    xmin[k] = q;
+    xmax[k] = q;
     partner[k] = int(k);
   }
 }
@@ -529,7 +531,8 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
                     const uint32_t *__restrict__ order, const BatchHeader *hdr,
                     const unsigned int *__restrict__ cell_base,
                     const SceneRecord *__restrict__ scenes, const uint32_t *__restrict__ seg_count,
-                    const uint32_t *__restrict__ seg_scan, float2 *__restrict__ sx,
+                    const uint32_t *__restrict__ seg_scan, float *__restrict__ xmin,
+                    float *__restrict__ xmax,
                     const float2 *__restrict__ cell_floor, float4 *__restrict__ syz,
                     int4 *__restrict__ sv, int *__restrict__ sflag, float2 *__restrict__ sfloor,
                     int *__restrict__ partner) {
@@ -570,7 +573,8 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
       }
       first = int64_t(a) + other;
     }
-    sx[k] = make_float2(x.min[g.axis], x.max[g.axis]);
+    xmin[k] = x.min[g.axis];
+    xmax[k] = x.max[g.axis];
     syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
     sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
     sflag[k] = (lo << 2) | (fc << 1) | fb;
@@ -665,7 +669,8 @@ cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, 
 
 cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
                                   int64_t slots_cap) {
-  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(scene.sx, scene.partner, hdr, slots_cap);
+  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(scene.xmin, scene.xmax, scene.partner, hdr,
+                                                                slots_cap);
   return cudaGetLastError();
 }
 
@@ -677,7 +682,7 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 float2 *cell_floor, int64_t cells_cap, SortedScene scene) {
   cell_floor_kernel<<<blocks_for(cells_cap), kBlock, 0, s>>>(cell_base, scenes, hdr, cell_floor, cells_cap);
   gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
-                                                             scenes, seg_count, seg_scan, scene.sx,
+                                                             scenes, seg_count, seg_scan, scene.xmin, scene.xmax,
                                                              cell_floor, scene.syz, scene.sv,
                                                              scene.sflag, scene.sfloor, scene.partner);
   return cudaGetLastError();

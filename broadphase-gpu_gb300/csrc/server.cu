@@ -380,7 +380,7 @@ int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t ma
   size_t free_b = 0, total = 0;
   cudaMemGetInfo(&free_b, &total);
   sv->fixed = int64_t(ctx->in_dev.bytes + ctx->counts.bytes + ctx->offsets.bytes + ctx->scan_ws.bytes +
-                      ctx->keys64[0].bytes * 2 + ctx->vals[0].bytes * 2 + ctx->sort_ws.bytes + ctx->sx.bytes +
+                      ctx->keys64[0].bytes * 2 + ctx->vals[0].bytes * 2 + ctx->sort_ws.bytes + ctx->xmin.bytes + ctx->xmax.bytes +
                       ctx->syz.bytes + ctx->sv.bytes + ctx->sflag.bytes + ctx->sfloor.bytes +
                       ctx->cell_floor.bytes + ctx->partner.bytes +
                       ctx->seg_count.bytes + ctx->seg_scan.bytes + ctx->batch_boxes.bytes);

@@ -27,8 +27,9 @@ constexpr size_t kOffVals0 = kOffKeys1 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kOffVals1 = kOffVals0 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kOffSortWs = kOffVals1 + up256(sizeof(uint32_t) * kMax);
 constexpr size_t kSortWsBytes = sizeof(uint32_t) * (256 * ((kMax + kRadixTile - 1) / kRadixTile) + 256) + 256;
-constexpr size_t kOffSx = kOffSortWs + up256(kSortWsBytes);
-constexpr size_t kOffSyz = kOffSx + up256(sizeof(float2) * kSlots);
+constexpr size_t kOffXmin = kOffSortWs + up256(kSortWsBytes);
+constexpr size_t kOffXmax = kOffXmin + up256(sizeof(float) * kSlots);
+constexpr size_t kOffSyz = kOffXmax + up256(sizeof(float) * kSlots);
 constexpr size_t kOffSv = kOffSyz + up256(sizeof(float4) * kSlots);
 constexpr size_t kOffFlag = kOffSv + up256(sizeof(int4) * kSlots);
 constexpr size_t kOffFloor = kOffFlag + up256(sizeof(int) * kSlots);
@@ -71,7 +72,8 @@ __global__ void static_keys_kernel(const stq_aabb *__restrict__ boxes, int n, in
 // Sorted positions 0..n-1 (one cell), then the NaN sentinel and the padding.
 __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, int axis,
                                      const uint32_t *__restrict__ order, unsigned char *scratch) {
-  float2 *sx = reinterpret_cast<float2 *>(scratch + kOffSx);
+  float *xmin = reinterpret_cast<float *>(scratch + kOffXmin);
+  float *xmax = reinterpret_cast<float *>(scratch + kOffXmax);
   float4 *syz = reinterpret_cast<float4 *>(scratch + kOffSyz);
   int4 *sv = reinterpret_cast<int4 *>(scratch + kOffSv);
   int *sflag = reinterpret_cast<int *>(scratch + kOffFlag);
@@ -81,7 +83,8 @@ __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, 
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) {
     const stq_aabb &x = boxes[order[k]];
-    sx[k] = make_float2(x.min[axis], x.max[axis]);
+    xmin[k] = x.min[axis];
+    xmax[k] = x.max[axis];
     syz[k] = make_float4(x.min[b], x.min[c], x.max[b], x.max[c]);
     sv[k] = make_int4(x.vertex_ids[0], x.vertex_ids[1], x.vertex_ids[2], x.id);
     sflag[k] = 3;  // one cell: every box is in its first cell on both axes
@@ -89,7 +92,8 @@ __global__ void static_gather_kernel(const stq_aabb *__restrict__ boxes, int n, 
     partner[k] = k + 1;  // one list: candidates follow in sort order
   } else if (k < n + 1 + kSortedPad) {
     const float q = __int_as_float(0x7fc00000);
-    sx[k] = make_float2(q, q);
+    xmin[k] = q;
+    xmax[k] = q;
     partner[k] = k;
   }
 }
@@ -137,7 +141,8 @@ extern "C" int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, st
     return STQ_ERR_CUDA;
   static_gather_kernel<<<blocks, 256, 0, s>>>(d_boxes, ni, axis, vb[which], scratch);
   SweepParams p;
-  p.sx = reinterpret_cast<const float2 *>(scratch + kOffSx);
+  p.xmin = reinterpret_cast<const float *>(scratch + kOffXmin);
+  p.xmax = reinterpret_cast<const float *>(scratch + kOffXmax);
   p.syz = reinterpret_cast<const float4 *>(scratch + kOffSyz);
   p.sv = reinterpret_cast<const int4 *>(scratch + kOffSv);
   p.sflag = reinterpret_cast<const int *>(scratch + kOffFlag);

@@ -139,9 +139,10 @@ struct SweepTuning {
 };
 
 // Sorted scene in HBM, structure of arrays, one sentinel after the boxes
-// (sx = NaN) followed by kSortedPad padding entries.
+// (xmin = xmax = NaN) followed by kSortedPad padding entries.
 struct SortedScene {
-  float2 *sx = nullptr;   // (min, max) on the sweep axis
+  float *xmin = nullptr;  // min on the sweep axis (all a candidate needs)
+  float *xmax = nullptr;  // max on the sweep axis (read once per start box)
   float4 *syz = nullptr;  // (min_b, min_c, max_b, max_c) on the other axes
   int4 *sv = nullptr;     // (vertexIds[0..2], id)
   int *sflag = nullptr;   // first-cell bits (0: along b, 1: along c), scene << 2
@@ -171,7 +172,8 @@ struct SweepCursors {
 };
 
 struct SweepParams {
-  const float2 *sx;
+  const float *xmin;
+  const float *xmax;
   const float4 *syz;
   const int4 *sv;
   int32_t begin, end;        // start positions [begin, min(end, hdr->length))

@@ -96,7 +96,7 @@ stq_sweep_kernel(const SweepParams p) {
       const int take = min(32, min(Q - qsize, chunk_end - next_k));
       const int kk = next_k + lane;
       bool push = false;
-      if (lane < take) push = p.sx[p.partner[kk]].x <= p.sx[kk].y;
+      if (lane < take) push = p.xmin[p.partner[kk]] <= p.xmax[kk];
       const unsigned m = __ballot_sync(kFullMask, push);
       if (push) q[(qhead + qsize + __popc(m & lanemask_lt())) & (Q - 1)] = kk;
       qsize += __popc(m);
@@ -112,7 +112,7 @@ stq_sweep_kernel(const SweepParams p) {
       if (r < ntake) {
         k = q[(qhead + r) & (Q - 1)];
         j0 = p.partner[k];
-        kmax = p.sx[k].y;
+        kmax = p.xmax[k];
         kb = p.syz[k];
         kv = p.sv[k];
         kfl = p.sfloor[k];
@@ -132,7 +132,7 @@ stq_sweep_kernel(const SweepParams p) {
     // 3. Test G consecutive candidates per group. Valid lanes form the
     //    prefix of the group before the first x-test failure.
     const int j = j0 + gl;
-    const bool xok = active && p.sx[j].x <= kmax;
+    const bool xok = active && p.xmin[j] <= kmax;
     const unsigned failm = __ballot_sync(kFullMask, active && !xok);
     const bool valid = active && (failm & upto_me) == 0;
     bool hit = false;
@@ -262,7 +262,7 @@ stq_sweep_lane_kernel(const SweepParams p) {
       const int take = min(32, min(Q - qsize, chunk_end - next_k));
       const int kk = next_k + lane;
       bool push = false;
-      if (lane < take) push = p.sx[p.partner[kk]].x <= p.sx[kk].y;
+      if (lane < take) push = p.xmin[p.partner[kk]] <= p.xmax[kk];
       const unsigned m = __ballot_sync(kFullMask, push);
       if (push) q[(qhead + qsize + __popc(m & below)) & (Q - 1)] = kk;
       qsize += __popc(m);
@@ -277,7 +277,7 @@ stq_sweep_lane_kernel(const SweepParams p) {
       if (r < ntake) {
         k = q[(qhead + r) & (Q - 1)];
         j = p.partner[k];
-        kmax = p.sx[k].y;
+        kmax = p.xmax[k];
         kb = p.syz[k];
         kv = p.sv[k];
         kfl = p.sfloor[k];
@@ -298,7 +298,7 @@ stq_sweep_lane_kernel(const SweepParams p) {
     //    the first x-test failure (a NaN sentinel ends every list).
     float xm[U];
 #pragma unroll
-    for (int u = 0; u < U; ++u) xm[u] = active ? p.sx[j + u].x : 0.f;
+    for (int u = 0; u < U; ++u) xm[u] = active ? p.xmin[j + u] : 0.f;
     int nvalid = 0;
     if (active) {
 #pragma unroll
@@ -412,7 +412,7 @@ stq_long_run_kernel(const SweepParams p) {
     const int2 it = p.long_list[item];
     const int k = it.x;
     int j = it.y;
-    const float kmax = p.sx[k].y;
+    const float kmax = p.xmax[k];
     const float4 kb = p.syz[k];
     const int4 kv = p.sv[k];
     const float2 kfl = p.sfloor[k];
@@ -421,7 +421,7 @@ stq_long_run_kernel(const SweepParams p) {
     while (true) {
       float xm[U];
 #pragma unroll
-      for (int u = 0; u < U; ++u) xm[u] = p.sx[j + 32 * u + lane].x;
+      for (int u = 0; u < U; ++u) xm[u] = p.xmin[j + 32 * u + lane];
       int first = 32 * U;  // offset of the first x-test failure
 #pragma unroll
       for (int u = 0; u < U; ++u) {
