@@ -18,6 +18,7 @@
 // shared-memory atomics, and one global atomic per warp step that emits.
 #include <map>
 #include <mutex>
+#include <type_traits>
 #include <utility>
 
 #include "stq_device.cuh"
@@ -221,12 +222,17 @@ stq_sweep_lane_kernel(const SweepParams p) {
   static_assert(U == 1 || U == 2 || U == 4 || U == 8, "candidates per lane step: 1, 2, 4 or 8");
   static_assert((Q & (Q - 1)) == 0 && Q >= 32, "queue depth: power of two >= 32");
   constexpr int STAGE = 32 * (U + 1);  // < 32 left over + at most 32 * U new pairs
-  __shared__ int ring[BLOCK / 32][Q];
+  // A ring entry carries the partner the refill read for its start box, so a
+  // take starts the candidate loads without a dependent global load; where
+  // that would pass 48 KB of shared memory the entry is the start box alone.
+  constexpr bool kWide = (BLOCK / 32) * (Q * 8 + STAGE * 8) <= 48 * 1024;
+  using Entry = typename std::conditional<kWide, int2, int>::type;
+  __shared__ Entry ring[BLOCK / 32][Q];
   __shared__ int2 stage[COUNT ? 1 : BLOCK / 32][COUNT ? 1 : STAGE];
 
   const int lane = threadIdx.x & 31;
   const unsigned below = lanemask_lt();
-  int *q = ring[threadIdx.x >> 5];
+  Entry *q = ring[threadIdx.x >> 5];
   int2 *st = stage[COUNT ? 0 : (threadIdx.x >> 5)];
 
   int qhead = 0, qsize = 0;
@@ -262,9 +268,17 @@ stq_sweep_lane_kernel(const SweepParams p) {
       const int take = min(32, min(Q - qsize, chunk_end - next_k));
       const int kk = next_k + lane;
       bool push = false;
-      if (lane < take) push = p.xmin[p.partner[kk]] <= p.xmax[kk];
+      int pk = 0;
+      if (lane < take) {
+        pk = p.partner[kk];
+        push = p.xmin[pk] <= p.xmax[kk];
+      }
       const unsigned m = __ballot_sync(kFullMask, push);
-      if (push) q[(qhead + qsize + __popc(m & below)) & (Q - 1)] = kk;
+      if (push) {
+        Entry &slot = q[(qhead + qsize + __popc(m & below)) & (Q - 1)];
+        if constexpr (kWide) slot = make_int2(kk, pk);
+        else slot = kk;
+      }
       qsize += __popc(m);
       next_k += take;
     }
@@ -275,8 +289,14 @@ stq_sweep_lane_kernel(const SweepParams p) {
     if (k < 0) {
       const int r = __popc(needm & below);
       if (r < ntake) {
-        k = q[(qhead + r) & (Q - 1)];
-        j = p.partner[k];
+        const Entry e = q[(qhead + r) & (Q - 1)];
+        if constexpr (kWide) {
+          k = e.x;
+          j = e.y;
+        } else {
+          k = e;
+          j = p.partner[k];
+        }
         kmax = p.xmax[k];
         kb = p.syz[k];
         kv = p.sv[k];
