@@ -939,80 +939,90 @@ int sweep_to_host(stq_context *ctx, stq_pair *h_pairs, int64_t capacity, int64_t
   };
   if (windows < 2 || capacity == 0 || ctx->options[STQ_OPT_HOST_OVERLAP] == 2) return one_copy();
 
-  STQ_CUDA(ctx, ctx->window_pairs.ensure(pair_bytes), "allocate pair staging");
-  STQ_CUDA(ctx, ctx->window_long_list.ensure(sizeof(int2) * size_t(ctx->slot_cap)), "allocate long-run list");
-  STQ_CUDA(ctx, ctx->window_cursors.ensure(2 * sizeof(WindowCounters)), "allocate window cursors");
-  for (cudaStream_t *st : {&ctx->copy_stream, &ctx->window_stream})
-    if (!*st) STQ_CUDA(ctx, cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "create stream");
-  if (!ctx->h_window_pairs) {
-    STQ_CUDA(ctx, cudaHostAlloc(&ctx->h_window_pairs, sizeof(unsigned long long) * stq_context::kCopyWindows,
-                                cudaHostAllocMapped),
-             "allocate window counters");
-    STQ_CUDA(ctx, cudaHostGetDevicePointer(&ctx->d_window_pairs, ctx->h_window_pairs, 0),
-             "map window counters");
-  }
-  for (cudaEvent_t *e : {&ctx->window_start, &ctx->window_done[0]})
-    if (!*e) STQ_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "create event");
-  for (int w = 1; w < windows; ++w)
-    if (!ctx->window_done[w])
-      STQ_CUDA(ctx, cudaEventCreateWithFlags(&ctx->window_done[w], cudaEventDisableTiming), "create event");
-
-  WindowCounters *wc = ctx->window_cursors.as<WindowCounters>();
-  stq_pair *slot_pairs[2] = {d_pairs, ctx->window_pairs.as<stq_pair>()};
-  int2 *slot_list[2] = {ctx->long_list.as<int2>(), ctx->window_long_list.as<int2>()};
-  cudaStream_t slot_stream[2] = {ctx->stream, ctx->window_stream};
-
-  // the header reset (candidate statistics) and the stage timer run on the
-  // context's stream; the second stream starts after them
-  STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, dev_hdr(ctx), ctx->scene_pairs.as<unsigned long long>(),
-                                   ctx->scene_cap),
-           "reset sweep");
-  ctx->launches += 1;
-  STQ_CUDA(ctx, cudaMemsetAsync(wc, 0, 2 * sizeof(WindowCounters), ctx->stream), "clear window cursors");
-  stage_begin(ctx, kSweep);
-  STQ_CUDA(ctx, cudaEventRecord(ctx->window_start, ctx->stream), "record window start");
-  STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->window_stream, ctx->window_start, 0), "order window stream");
-  for (int w = 0; w < windows; ++w) {
-    const int slot = w & 1;
-    cudaStream_t s = slot_stream[slot];
-    const SweepCursors cur{&wc[slot].pairs, &wc[slot].work, slot_list[slot], &wc[slot].long_items,
-                           &wc[slot].long_work};
-    const int64_t b = length * w / windows, e = length * (w + 1) / windows;
-    STQ_TRY(run_sweep(ctx, b, e, slot_pairs[slot], capacity, false, false, &cur, s));
-    // the count to the host by a kernel store: a copy here would wait behind
-    // the pair copies on the copy engines and hold up this stream's next window
-    STQ_CUDA(ctx, launch_window_step(s, &wc[slot], ctx->d_window_pairs + w), "publish window count");
-    ctx->launches += 1;
-    STQ_CUDA(ctx, cudaEventRecord(ctx->window_done[w], s), "record window");
-  }
-  // the stage (and the header read below) ends when both streams have
-  for (int w = windows - 2; w < windows; ++w)
-    STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->window_done[w], 0), "join window streams");
-  stage_end(ctx, kSweep);
-  int64_t done = 0;
-  for (int w = 0; w < windows; ++w) {
-    STQ_CUDA(ctx, cudaEventSynchronize(ctx->window_done[w]), "wait for sweep window");
-    const volatile unsigned long long *hc = ctx->h_window_pairs;
-    const int64_t from = w >= 2 ? int64_t(hc[w - 2]) : 0;
-    const int64_t c = int64_t(hc[w]) - from;
-    if (c > capacity - done) {
-      // overflow: let the windows in flight end, then take the prefix rule
-      for (cudaStream_t st : {ctx->window_stream, ctx->stream, ctx->copy_stream})
-        STQ_CUDA(ctx, cudaStreamSynchronize(st), "synchronise window streams");
-      return one_copy();
+  auto windowed = [&]() -> int {
+    STQ_CUDA(ctx, ctx->window_pairs.ensure(pair_bytes), "allocate pair staging");
+    STQ_CUDA(ctx, ctx->window_long_list.ensure(sizeof(int2) * size_t(ctx->slot_cap)), "allocate long-run list");
+    STQ_CUDA(ctx, ctx->window_cursors.ensure(2 * sizeof(WindowCounters)), "allocate window cursors");
+    for (cudaStream_t *st : {&ctx->copy_stream, &ctx->window_stream})
+      if (!*st) STQ_CUDA(ctx, cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "create stream");
+    if (!ctx->h_window_pairs) {
+      STQ_CUDA(ctx, cudaHostAlloc(&ctx->h_window_pairs, sizeof(unsigned long long) * stq_context::kCopyWindows,
+                                  cudaHostAllocMapped),
+               "allocate window counters");
+      STQ_CUDA(ctx, cudaHostGetDevicePointer(&ctx->d_window_pairs, ctx->h_window_pairs, 0),
+               "map window counters");
     }
-    if (c > 0)
-      STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs + done, slot_pairs[w & 1] + from, sizeof(stq_pair) * size_t(c),
-                                    cudaMemcpyDeviceToHost, ctx->copy_stream),
-               "copy window pairs to host");
-    done += c;
+    for (cudaEvent_t *e : {&ctx->window_start, &ctx->window_done[0]})
+      if (!*e) STQ_CUDA(ctx, cudaEventCreateWithFlags(e, cudaEventDisableTiming), "create event");
+    for (int w = 1; w < windows; ++w)
+      if (!ctx->window_done[w])
+        STQ_CUDA(ctx, cudaEventCreateWithFlags(&ctx->window_done[w], cudaEventDisableTiming), "create event");
+
+    WindowCounters *wc = ctx->window_cursors.as<WindowCounters>();
+    stq_pair *slot_pairs[2] = {d_pairs, ctx->window_pairs.as<stq_pair>()};
+    int2 *slot_list[2] = {ctx->long_list.as<int2>(), ctx->window_long_list.as<int2>()};
+    cudaStream_t slot_stream[2] = {ctx->stream, ctx->window_stream};
+
+    // the header reset (candidate statistics) and the stage timer run on the
+    // context's stream; the second stream starts after them
+    STQ_CUDA(ctx, launch_reset_sweep(ctx->stream, dev_hdr(ctx), ctx->scene_pairs.as<unsigned long long>(),
+                                     ctx->scene_cap),
+             "reset sweep");
+    ctx->launches += 1;
+    STQ_CUDA(ctx, cudaMemsetAsync(wc, 0, 2 * sizeof(WindowCounters), ctx->stream), "clear window cursors");
+    stage_begin(ctx, kSweep);
+    STQ_CUDA(ctx, cudaEventRecord(ctx->window_start, ctx->stream), "record window start");
+    STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->window_stream, ctx->window_start, 0), "order window stream");
+    for (int w = 0; w < windows; ++w) {
+      const int slot = w & 1;
+      cudaStream_t s = slot_stream[slot];
+      const SweepCursors cur{&wc[slot].pairs, &wc[slot].work, slot_list[slot], &wc[slot].long_items,
+                             &wc[slot].long_work};
+      const int64_t b = length * w / windows, e = length * (w + 1) / windows;
+      STQ_TRY(run_sweep(ctx, b, e, slot_pairs[slot], capacity, false, false, &cur, s));
+      // the count to the host by a kernel store: a copy here would wait behind
+      // the pair copies on the copy engines and hold up this stream's next window
+      STQ_CUDA(ctx, launch_window_step(s, &wc[slot], ctx->d_window_pairs + w), "publish window count");
+      ctx->launches += 1;
+      STQ_CUDA(ctx, cudaEventRecord(ctx->window_done[w], s), "record window");
+    }
+    // the stage (and the header read below) ends when both streams have
+    for (int w = windows - 2; w < windows; ++w)
+      STQ_CUDA(ctx, cudaStreamWaitEvent(ctx->stream, ctx->window_done[w], 0), "join window streams");
+    stage_end(ctx, kSweep);
+    int64_t done = 0;
+    for (int w = 0; w < windows; ++w) {
+      STQ_CUDA(ctx, cudaEventSynchronize(ctx->window_done[w]), "wait for sweep window");
+      const volatile unsigned long long *hc = ctx->h_window_pairs;
+      const int64_t from = w >= 2 ? int64_t(hc[w - 2]) : 0;
+      const int64_t c = int64_t(hc[w]) - from;
+      if (c > capacity - done) {
+        // overflow: let the windows in flight end, then take the prefix rule
+        for (cudaStream_t st : {ctx->window_stream, ctx->stream, ctx->copy_stream})
+          STQ_CUDA(ctx, cudaStreamSynchronize(st), "synchronise window streams");
+        return one_copy();
+      }
+      if (c > 0)
+        STQ_CUDA(ctx, cudaMemcpyAsync(h_pairs + done, slot_pairs[w & 1] + from, sizeof(stq_pair) * size_t(c),
+                                      cudaMemcpyDeviceToHost, ctx->copy_stream),
+                 "copy window pairs to host");
+      done += c;
+    }
+    STQ_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream), "synchronise copy stream");
+    STQ_TRY(read_header(ctx));  // waits for both streams (joined above); input flags
+    ctx->h_hdr->pairs = (unsigned long long)done;
+    if (total) *total = done;
+    *count = done;
+    return STQ_OK;
+  };
+  const int st = windowed();
+  if (st != STQ_OK && st != STQ_OVERFLOW) {
+    // an error can leave windows in flight on the second stream and copies on
+    // the third: wait for them, so that no later call on this context races them
+    for (cudaStream_t sm : {ctx->window_stream, ctx->copy_stream, ctx->stream})
+      if (sm) cudaStreamSynchronize(sm);
   }
-  STQ_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream), "synchronise copy stream");
-  STQ_TRY(read_header(ctx));  // waits for both streams (joined above); input flags
-  ctx->h_hdr->pairs = (unsigned long long)done;
-  if (total) *total = done;
-  *count = done;
-  return STQ_OK;
+  return st;
 }
 
 }  // namespace
