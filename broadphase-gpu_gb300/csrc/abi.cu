@@ -199,7 +199,6 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
   b.box_keys2 = ctx->bkeys[1].as<uint32_t>();
   b.box_vals2 = ctx->bvals[1].as<uint32_t>();
   b.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
-  b.seg_count = ctx->seg_count.as<uint32_t>();
   b.seg_scan = ctx->seg_scan.as<uint32_t>();
   b.seg_cap = ctx->seg_cap;
   b.box_cap = ctx->box_cap;
@@ -235,9 +234,7 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
            "allocate sort workspace");
   // three lists (vertices, edges, faces) per cell, each followed by a sentinel
   const int64_t segs = std::max<int64_t>(3 * cells_cap, ctx->seg_cap);
-  STQ_CUDA(ctx, ctx->seg_count.ensure(sizeof(uint32_t) * size_t(segs)), "allocate segment counts");
   STQ_CUDA(ctx, ctx->seg_scan.ensure(sizeof(uint32_t) * size_t(segs + 1)), "allocate segment offsets");
-  STQ_CUDA(ctx, ctx->seg_scan_ws.ensure(scan_workspace_bytes(segs) + 16), "allocate segment scan");
   ctx->seg_cap = segs;
   const size_t slots = r + size_t(segs) + 1 + kSortedPad;
   STQ_CUDA(ctx, ctx->xmin.ensure(sizeof(float) * slots), "allocate sorted scene");
@@ -289,17 +286,10 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_box
 
 int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, int64_t n_boxes,
                          int64_t replicas) {
-  STQ_CUDA(ctx, cudaMemsetAsync(b.seg_count, 0, sizeof(uint32_t) * size_t(b.seg_cap), ctx->stream),
-           "clear segment counts");
   BatchBuffers bs = b;
   bs.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
   STQ_CUDA(ctx, launch_batch_emit(ctx->stream, bs, n_boxes >= 0 ? n_boxes : ctx->box_cap, ctx->num_sms),
            "launch replica emit");
-  uint32_t *seg_total = reinterpret_cast<uint32_t *>(ctx->seg_scan_ws.as<char>() +
-                                                     scan_workspace_bytes(b.seg_cap));
-  STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.seg_count, b.seg_scan, b.seg_cap,
-                                   ctx->seg_scan_ws.ptr, seg_total, &ctx->launches),
-           "launch segment scan");
   stage_end(ctx, kKeys);
   // the replicas arrive in sweep-axis order: a stable sort by list id alone
   // (the key's high half) leaves every list sorted by its minima
@@ -322,10 +312,11 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   ctx->scene.sfloor = ctx->sfloor.as<float2>();
   ctx->scene.partner = ctx->partner.as<int>();
   stage_begin(ctx, kGather);
+  STQ_CUDA(ctx, launch_list_offsets(ctx->stream, kb[which], b.hdr, b.seg_scan, b.seg_cap), "launch list offsets");
   STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene, b.hdr, ctx->slot_cap),
            "launch sentinel fill");
   STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, r, b.cell_base, b.scenes,
-                                    b.seg_count, b.seg_scan, ctx->cell_floor.as<float2>(), ctx->seg_cap / 3,
+                                    b.seg_scan, ctx->cell_floor.as<float2>(), ctx->seg_cap / 3,
                                     ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
@@ -470,7 +461,7 @@ void stq_context_destroy(stq_context *ctx) {
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
                       &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
-                      &ctx->seg_count, &ctx->seg_scan, &ctx->seg_scan_ws, &ctx->bkeys[0], &ctx->bkeys[1],
+                      &ctx->seg_scan, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
                       &ctx->batch_boxes, &ctx->e2e_boxes, &ctx->e2e_pairs, &ctx->e2e_mesh, &ctx->aux,

@@ -395,14 +395,13 @@ batch_count_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restric
 
 // ---- 6. replica keys: (segment << 32) | order-preserving min, where the
 // segment is (global cell, box type): every cell holds a vertex, an edge and
-// a face list. Also counts replicas per segment.
+// a face list.
 __global__ void __launch_bounds__(kBlock)
 batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict__ order,
                   const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
                   const unsigned int *__restrict__ cell_base, BatchHeader *hdr,
                   const uint32_t *__restrict__ offsets, unsigned long long *__restrict__ keys,
-                  uint32_t *__restrict__ vals, uint32_t *__restrict__ seg_count, long long rep_cap,
-                  long long seg_cap) {
+                  uint32_t *__restrict__ vals, long long rep_cap, long long seg_cap) {
   const bool fits = (long long)hdr->replicas <= rep_cap && 3ll * hdr->cells <= seg_cap;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     // each of the 3 lists of a cell is followed by its sentinel; the last
@@ -434,7 +433,6 @@ batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict
         const unsigned long long seg = (cb0 + (unsigned long long)(cb * g.nc + cc)) * 3ull + type;
         keys[o] = (seg << 32) | xk;
         vals[o] = bi;
-        atomicAdd(&seg_count[seg], 1u);
         ++o;
       }
   }
@@ -456,13 +454,31 @@ batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restr
   }
 }
 
-// Longest (cell, type) list, a statistic of the prepared scene.
+// First position of every (cell, type) list in the sorted replicas, and one
+// entry past the last (the replica count): the keys are sorted by list id, so
+// each offset is the lower bound of its id. Also the longest list, a
+// statistic of the prepared scene.
 __global__ void __launch_bounds__(kBlock)
-list_max_kernel(const uint32_t *__restrict__ seg_count, BatchHeader *__restrict__ hdr, long long seg_cap) {
+list_offsets_kernel(const unsigned long long *__restrict__ keys, BatchHeader *__restrict__ hdr,
+                    uint32_t *__restrict__ seg_scan, long long seg_cap) {
   // nothing was emitted past the capacity (the emit flags that overflow)
   const uint32_t nseg = uint32_t(min(3ll * hdr->cells, seg_cap));
+  const uint32_t R = hdr->replicas;
   uint32_t mx = 0;
-  for (uint32_t s = blockIdx.x * kBlock + threadIdx.x; s < nseg; s += gridDim.x * kBlock) mx = max(mx, seg_count[s]);
+  auto lower = [&](uint32_t s) {
+    uint32_t a = 0, e = R;
+    while (a < e) {
+      const uint32_t mid = (a + e) >> 1;
+      if (uint32_t(keys[mid] >> 32) < s) a = mid + 1;
+      else e = mid;
+    }
+    return a;
+  };
+  for (uint32_t s = blockIdx.x * kBlock + threadIdx.x; s <= nseg; s += gridDim.x * kBlock) {
+    const uint32_t lo = s < nseg ? lower(s) : R;
+    seg_scan[s] = lo;
+    if (s < nseg) mx = max(mx, lower(s + 1) - lo);
+  }
   mx = __reduce_max_sync(kFullMask, mx);
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(&hdr->max_list, mx);
 }
@@ -530,8 +546,8 @@ __global__ void __launch_bounds__(kBlock)
 gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long *__restrict__ keys,
                     const uint32_t *__restrict__ order, const BatchHeader *hdr,
                     const unsigned int *__restrict__ cell_base,
-                    const SceneRecord *__restrict__ scenes, const uint32_t *__restrict__ seg_count,
-                    const uint32_t *__restrict__ seg_scan, float *__restrict__ xmin,
+                    const SceneRecord *__restrict__ scenes, const uint32_t *__restrict__ seg_scan,
+                    float *__restrict__ xmin,
                     float *__restrict__ xmax,
                     const float2 *__restrict__ cell_floor, float4 *__restrict__ syz,
                     int4 *__restrict__ sv, int *__restrict__ sflag, float2 *__restrict__ sfloor,
@@ -564,7 +580,7 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
       // bound search of this min among the other list's sorted keys
       const unsigned int other = 3u * cell + (type == 0u ? 2u : 0u);
       const uint32_t xk = uint32_t(key & 0xffffffffu);
-      uint32_t a = seg_scan[other], e = a + seg_count[other];
+      uint32_t a = seg_scan[other], e = seg_scan[other + 1];
       while (a < e) {
         const uint32_t mid = (a + e) >> 1;
         const uint32_t mk = uint32_t(keys[mid] & 0xffffffffu);
@@ -662,8 +678,13 @@ cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n
 
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms) {
   batch_emit_kernel<<<blocks_for(n), kBlock, 0, s>>>(b.boxes, b.order, b.box_off, b.scenes, b.cell_base, b.hdr,
-                                              b.offsets, b.keys, b.vals, b.seg_count, b.rep_cap, b.seg_cap);
-  list_max_kernel<<<unsigned(num_sms * 2), kBlock, 0, s>>>(b.seg_count, b.hdr, b.seg_cap);
+                                              b.offsets, b.keys, b.vals, b.rep_cap, b.seg_cap);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_list_offsets(cudaStream_t s, const unsigned long long *keys, BatchHeader *hdr, uint32_t *seg_scan,
+                                int64_t seg_cap) {
+  list_offsets_kernel<<<blocks_for(seg_cap + 1), kBlock, 0, s>>>(keys, hdr, seg_scan, seg_cap);
   return cudaGetLastError();
 }
 
@@ -678,11 +699,11 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
-                                const uint32_t *seg_count, const uint32_t *seg_scan,
-                                float2 *cell_floor, int64_t cells_cap, SortedScene scene) {
+                                const uint32_t *seg_scan, float2 *cell_floor, int64_t cells_cap,
+                                SortedScene scene) {
   cell_floor_kernel<<<blocks_for(cells_cap), kBlock, 0, s>>>(cell_base, scenes, hdr, cell_floor, cells_cap);
   gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
-                                                             scenes, seg_count, seg_scan, scene.xmin, scene.xmax,
+                                                             scenes, seg_scan, scene.xmin, scene.xmax,
                                                              cell_floor, scene.syz, scene.sv,
                                                              scene.sflag, scene.sfloor, scene.partner);
   return cudaGetLastError();

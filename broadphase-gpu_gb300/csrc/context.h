@@ -77,7 +77,7 @@ struct stq_context {
   DevBuf xmin, xmax, syz, sv, sflag, sfloor, partner, box_counts, prefix_ws, pair_keys[2];
   DevBuf cell_floor;  // lower bounds of each cell on b and c
   DevBuf long_list;  // runs handed from the lane sweep to the warp pass
-  DevBuf seg_count, seg_scan, seg_scan_ws;  // replicas per (cell, type) list
+  DevBuf seg_scan;  // first sorted replica of each (cell, type) list
   DevBuf bkeys[2], bvals[2];  // box sort: keys and box indices, double-buffered
   int order_buf = 0;          // which bvals buffer holds the sorted box order
   int64_t seg_cap = 0;

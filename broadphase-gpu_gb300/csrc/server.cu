@@ -383,7 +383,7 @@ int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t ma
                       ctx->keys64[0].bytes * 2 + ctx->vals[0].bytes * 2 + ctx->sort_ws.bytes + ctx->xmin.bytes + ctx->xmax.bytes +
                       ctx->syz.bytes + ctx->sv.bytes + ctx->sflag.bytes + ctx->sfloor.bytes +
                       ctx->cell_floor.bytes + ctx->partner.bytes +
-                      ctx->seg_count.bytes + ctx->seg_scan.bytes + ctx->batch_boxes.bytes);
+                      ctx->seg_scan.bytes + ctx->batch_boxes.bytes);
   if (sv->fixed >= budget_bytes) return bad(STQ_ERR_NO_MEMORY);
   *out = sv.release();
   return STQ_OK;

@@ -224,8 +224,8 @@ struct BatchBuffers {
   const uint32_t *order;        // boxes in sweep-axis order (box sort output)
   unsigned long long *keys;     // replica keys (sort input)
   uint32_t *vals;               // replica box indices (sort input)
-  uint32_t *seg_count;          // replicas per segment (cell x type), seg_cap entries
-  uint32_t *seg_scan;           // exclusive scan of seg_count
+  uint32_t *seg_scan;           // first sorted replica of each segment (cell x type),
+                                // seg_cap + 1 entries
   long long seg_cap;
   long long box_cap;            // capacities
   long long rep_cap;
@@ -238,6 +238,9 @@ cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b);
 // device knows the count)
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n);
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms);
+// list offsets from the list-sorted keys (and the longest list)
+cudaError_t launch_list_offsets(cudaStream_t s, const unsigned long long *keys, BatchHeader *hdr, uint32_t *seg_scan,
+                                int64_t seg_cap);
 
 cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
                                   int64_t slots_cap);
@@ -245,8 +248,8 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
                                 const BatchHeader *hdr, int64_t rep_cap,
                                 const unsigned int *cell_base, const SceneRecord *scenes,
-                                const uint32_t *seg_count, const uint32_t *seg_scan,
-                                float2 *cell_floor, int64_t cells_cap, SortedScene scene);
+                                const uint32_t *seg_scan, float2 *cell_floor, int64_t cells_cap,
+                                SortedScene scene);
 // Batched box build: scene s has vertices [voff[s], voff[s+1]) etc.; box ids
 // are global (box_off[s] + local), vertex ids local to the scene.
 cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V1,
