@@ -78,20 +78,46 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total, uint32_t *
   return warp_base + x - v;
 }
 
-// One block per digit: exclusive scan of hist[d][0..ntiles) in place.
+// One block per digit: exclusive scan of hist[d][0..ntiles) in place, 8
+// entries per thread and block scan: coalesced loads into shared memory, each
+// thread scans 8 consecutive entries (padded indices: no bank conflicts).
 __global__ void __launch_bounds__(kSortBlock)
 scan_rows_kernel(uint32_t *__restrict__ hist, int64_t ntiles,
                  uint32_t *__restrict__ totals) {
+  constexpr int PER = 8, CHUNK = kSortBlock * PER;
+  __shared__ uint32_t buf[CHUNK + CHUNK / 32];
   __shared__ uint32_t scratch[32];
+  auto at = [](int x) { return x + (x >> 5); };
   uint32_t *row = hist + int64_t(blockIdx.x) * ntiles;
   uint32_t carry = 0;
-  for (int64_t b = 0; b < ntiles; b += kSortBlock) {
-    const int64_t i = b + threadIdx.x;
-    const uint32_t v = i < ntiles ? row[i] : 0;
+  for (int64_t b = 0; b < ntiles; b += CHUNK) {
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int x = i * kSortBlock + threadIdx.x;
+      buf[at(x)] = b + x < ntiles ? row[b + x] : 0u;
+    }
+    __syncthreads();
+    uint32_t v[PER], sum = 0;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      v[i] = buf[at(threadIdx.x * PER + i)];
+      sum += v[i];
+    }
     uint32_t tot;
-    const uint32_t ex = block_exclusive_scan(v, &tot, scratch);
-    if (i < ntiles) row[i] = carry + ex;
+    uint32_t run = carry + block_exclusive_scan(sum, &tot, scratch);
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      buf[at(threadIdx.x * PER + i)] = run;
+      run += v[i];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int x = i * kSortBlock + threadIdx.x;
+      if (b + x < ntiles) row[b + x] = buf[at(x)];
+    }
     carry += tot;
+    __syncthreads();  // the next chunk overwrites buf
   }
   if (threadIdx.x == 0) totals[blockIdx.x] = carry;
 }
