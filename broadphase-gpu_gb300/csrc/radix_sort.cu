@@ -78,48 +78,57 @@ __device__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *total, uint32_t *
   return warp_base + x - v;
 }
 
-// One block per digit: exclusive scan of hist[d][0..ntiles) in place, 8
-// entries per thread and block scan: coalesced loads into shared memory, each
-// thread scans 8 consecutive entries (padded indices: no bank conflicts).
+// Exclusive scan of in[b, b + 2048) (clipped to n) into out, starting from
+// carry, by one block with 8 entries per thread: coalesced loads into shared
+// memory, each thread scans 8 consecutive entries (padded indices: no bank
+// conflicts), one block scan. Returns the chunk's total (in every thread).
+constexpr int kChunkPer = 8, kChunk = kSortBlock * kChunkPer;
+__device__ uint32_t scan_chunk(const uint32_t *in, uint32_t *out, int64_t b, int64_t n, uint32_t carry) {
+  __shared__ uint32_t buf[kChunk + kChunk / 32];
+  __shared__ uint32_t scratch[32];
+  auto at = [](int x) { return x + (x >> 5); };
+#pragma unroll
+  for (int i = 0; i < kChunkPer; ++i) {
+    const int x = i * kSortBlock + threadIdx.x;
+    buf[at(x)] = b + x < n ? in[b + x] : 0u;
+  }
+  __syncthreads();
+  uint32_t v[kChunkPer], sum = 0;
+#pragma unroll
+  for (int i = 0; i < kChunkPer; ++i) {
+    v[i] = buf[at(threadIdx.x * kChunkPer + i)];
+    sum += v[i];
+  }
+  uint32_t tot;
+  uint32_t run = carry + block_exclusive_scan(sum, &tot, scratch);
+#pragma unroll
+  for (int i = 0; i < kChunkPer; ++i) {
+    buf[at(threadIdx.x * kChunkPer + i)] = run;
+    run += v[i];
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < kChunkPer; ++i) {
+    const int x = i * kSortBlock + threadIdx.x;
+    if (b + x < n) out[b + x] = buf[at(x)];
+  }
+  __syncthreads();  // the next chunk overwrites buf
+  return tot;
+}
+
+// Exclusive scan of row[0..n) in place by one block; returns the total.
+__device__ uint32_t block_scan_row(uint32_t *row, int64_t n) {
+  uint32_t carry = 0;
+  for (int64_t b = 0; b < n; b += kChunk) carry += scan_chunk(row, row, b, n, carry);
+  return carry;
+}
+
+// One block per digit: exclusive scan of hist[d][0..ntiles) in place.
 __global__ void __launch_bounds__(kSortBlock)
 scan_rows_kernel(uint32_t *__restrict__ hist, int64_t ntiles,
                  uint32_t *__restrict__ totals) {
-  constexpr int PER = 8, CHUNK = kSortBlock * PER;
-  __shared__ uint32_t buf[CHUNK + CHUNK / 32];
-  __shared__ uint32_t scratch[32];
-  auto at = [](int x) { return x + (x >> 5); };
-  uint32_t *row = hist + int64_t(blockIdx.x) * ntiles;
-  uint32_t carry = 0;
-  for (int64_t b = 0; b < ntiles; b += CHUNK) {
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      const int x = i * kSortBlock + threadIdx.x;
-      buf[at(x)] = b + x < ntiles ? row[b + x] : 0u;
-    }
-    __syncthreads();
-    uint32_t v[PER], sum = 0;
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      v[i] = buf[at(threadIdx.x * PER + i)];
-      sum += v[i];
-    }
-    uint32_t tot;
-    uint32_t run = carry + block_exclusive_scan(sum, &tot, scratch);
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      buf[at(threadIdx.x * PER + i)] = run;
-      run += v[i];
-    }
-    __syncthreads();
-#pragma unroll
-    for (int i = 0; i < PER; ++i) {
-      const int x = i * kSortBlock + threadIdx.x;
-      if (b + x < ntiles) row[b + x] = buf[at(x)];
-    }
-    carry += tot;
-    __syncthreads();  // the next chunk overwrites buf
-  }
-  if (threadIdx.x == 0) totals[blockIdx.x] = carry;
+  const uint32_t total = block_scan_row(hist + int64_t(blockIdx.x) * ntiles, ntiles);
+  if (threadIdx.x == 0) totals[blockIdx.x] = total;
 }
 
 template <int BINS>
@@ -304,10 +313,11 @@ constexpr int kScanTile = kSortBlock * kScanItems;
 __global__ void __launch_bounds__(kSortBlock)
 scan_reduce_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restrict__ sums) {
   __shared__ uint32_t scratch[32];
-  const int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
+  const int64_t base = int64_t(blockIdx.x) * kScanTile + threadIdx.x;
   uint32_t s = 0;
-  for (int i = 0; i < kScanItems; ++i)
-    if (base + i < n) s += in[base + i];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)  // coalesced; a sum needs no order
+    if (base + i * kSortBlock < n) s += in[base + i * kSortBlock];
   uint32_t tot;
   block_exclusive_scan(s, &tot, scratch);
   if (threadIdx.x == 0) sums[blockIdx.x] = tot;
@@ -315,36 +325,15 @@ scan_reduce_kernel(const uint32_t *__restrict__ in, int64_t n, uint32_t *__restr
 
 __global__ void __launch_bounds__(kSortBlock)
 scan_sums_kernel(uint32_t *__restrict__ sums, int64_t ntiles, uint32_t *__restrict__ total) {
-  __shared__ uint32_t scratch[32];
-  uint32_t carry = 0;
-  for (int64_t b = 0; b < ntiles; b += kSortBlock) {
-    const int64_t i = b + threadIdx.x;
-    const uint32_t v = i < ntiles ? sums[i] : 0;
-    uint32_t tot;
-    const uint32_t ex = block_exclusive_scan(v, &tot, scratch);
-    if (i < ntiles) sums[i] = carry + ex;
-    carry += tot;
-  }
-  if (threadIdx.x == 0) *total = carry;
+  const uint32_t t = block_scan_row(sums, ntiles);
+  if (threadIdx.x == 0) *total = t;
 }
 
 __global__ void __launch_bounds__(kSortBlock)
 scan_apply_kernel(const uint32_t *__restrict__ in, int64_t n, const uint32_t *__restrict__ sums,
                   uint32_t *__restrict__ out) {
-  __shared__ uint32_t scratch[32];
-  const int64_t base = int64_t(blockIdx.x) * kScanTile + int64_t(threadIdx.x) * kScanItems;
-  uint32_t v[kScanItems];
-  uint32_t s = 0;
-  for (int i = 0; i < kScanItems; ++i) {
-    v[i] = base + i < n ? in[base + i] : 0;
-    s += v[i];
-  }
-  uint32_t tot;
-  uint32_t run = sums[blockIdx.x] + block_exclusive_scan(s, &tot, scratch);
-  for (int i = 0; i < kScanItems; ++i) {
-    if (base + i < n) out[base + i] = run;
-    run += v[i];
-  }
+  static_assert(kScanTile == kChunk, "one chunk per scan tile");
+  scan_chunk(in, out, int64_t(blockIdx.x) * kScanTile, n, sums[blockIdx.x]);
 }
 
 }  // namespace
