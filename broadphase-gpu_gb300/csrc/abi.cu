@@ -312,15 +312,14 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   ctx->scene.sfloor = ctx->sfloor.as<float2>();
   ctx->scene.partner = ctx->partner.as<int>();
   stage_begin(ctx, kGather);
-  STQ_CUDA(ctx, launch_list_offsets(ctx->stream, kb[which], b.hdr, b.seg_scan, b.seg_cap), "launch list offsets");
-  STQ_CUDA(ctx, launch_fill_sentinels(ctx->stream, ctx->scene, b.hdr, ctx->slot_cap),
-           "launch sentinel fill");
+  STQ_CUDA(ctx, launch_list_offsets(ctx->stream, kb[which], b.hdr, b.seg_scan, b.seg_cap, ctx->scene, ctx->slot_cap),
+           "launch list offsets");
   STQ_CUDA(ctx, launch_gather_cells(ctx->stream, b.boxes, kb[which], vb[which], b.hdr, r, b.cell_base, b.scenes,
                                     b.seg_scan, ctx->cell_floor.as<float2>(), ctx->seg_cap / 3,
                                     ctx->scene),
            "launch gather");
   stage_end(ctx, kGather);
-  ctx->launches += 5;
+  ctx->launches += 4;
   return STQ_OK;
 }
 

@@ -456,14 +456,27 @@ batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restr
 
 // First position of every (cell, type) list in the sorted replicas, and one
 // entry past the last (the replica count): the keys are sorted by list id, so
-// each offset is the lower bound of its id. Also the longest list, a
-// statistic of the prepared scene.
+// each offset is the lower bound of its id. Sorted replica p of list s sits at
+// position p + s, so list s ends at position offset[s + 1] + s: the slot after
+// it gets the NaN sentinel (NaN bounds end every run there; its partner is
+// itself, so the sweep's refill test of a sentinel reads inside the scene and
+// fails), and so do kSortedPad slots of padding after the last list. The
+// gather writes every other position. Also the longest list, a statistic of
+// the prepared scene.
 __global__ void __launch_bounds__(kBlock)
 list_offsets_kernel(const unsigned long long *__restrict__ keys, BatchHeader *__restrict__ hdr,
-                    uint32_t *__restrict__ seg_scan, long long seg_cap) {
+                    uint32_t *__restrict__ seg_scan, long long seg_cap, SortedScene scene, int64_t slots_cap) {
   // nothing was emitted past the capacity (the emit flags that overflow)
   const uint32_t nseg = uint32_t(min(3ll * hdr->cells, seg_cap));
   const uint32_t R = hdr->replicas;
+  const float q = __int_as_float(0x7fc00000);
+  auto sentinel = [&](int64_t k) {
+    if (k < slots_cap) {
+      scene.xmin[k] = q;
+      scene.xmax[k] = q;
+      scene.partner[k] = int(k);
+    }
+  };
   uint32_t mx = 0;
   auto lower = [&](uint32_t s) {
     uint32_t a = 0, e = R;
@@ -474,30 +487,20 @@ list_offsets_kernel(const unsigned long long *__restrict__ keys, BatchHeader *__
     }
     return a;
   };
-  for (uint32_t s = blockIdx.x * kBlock + threadIdx.x; s <= nseg; s += gridDim.x * kBlock) {
+  const uint32_t stride = gridDim.x * kBlock;
+  for (uint32_t s = blockIdx.x * kBlock + threadIdx.x; s <= nseg; s += stride) {
     const uint32_t lo = s < nseg ? lower(s) : R;
     seg_scan[s] = lo;
-    if (s < nseg) mx = max(mx, lower(s + 1) - lo);
+    if (s < nseg) {
+      const uint32_t hi = lower(s + 1);
+      mx = max(mx, hi - lo);
+      sentinel(int64_t(hi) + s);
+    }
   }
+  for (uint32_t t = blockIdx.x * kBlock + threadIdx.x; t < uint32_t(kSortedPad); t += stride)
+    sentinel(int64_t(R) + nseg + t);
   mx = __reduce_max_sync(kFullMask, mx);
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(&hdr->max_list, mx);
-}
-
-__global__ void __launch_bounds__(kBlock)
-fill_sentinels_kernel(float *__restrict__ xmin, float *__restrict__ xmax, int *__restrict__ partner,
-                      const BatchHeader *hdr,
-                      int64_t slots_cap) {
-  const int64_t slots = min(slots_cap, int64_t(hdr->length) + 1 + kSortedPad);
-  const float q = __int_as_float(0x7fc00000);
-  // every position a sentinel until the gather writes the replicas: NaN
-  // bounds, and a partner that points at itself, so that the sweep's refill
-  // test of a sentinel position reads inside the scene (and fails)
-  for (int64_t k = blockIdx.x * int64_t(kBlock) + threadIdx.x; k < slots;
-       k += int64_t(gridDim.x) * kBlock) {
-    xmin[k] = q;
-    xmax[k] = q;
-    partner[k] = int(k);
-  }
 }
 
 // Lower bounds of every cell on the two non-sweep axes (-inf for the first
@@ -683,15 +686,8 @@ cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, 
 }
 
 cudaError_t launch_list_offsets(cudaStream_t s, const unsigned long long *keys, BatchHeader *hdr, uint32_t *seg_scan,
-                                int64_t seg_cap) {
-  list_offsets_kernel<<<blocks_for(seg_cap + 1), kBlock, 0, s>>>(keys, hdr, seg_scan, seg_cap);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
-                                  int64_t slots_cap) {
-  fill_sentinels_kernel<<<blocks_for(slots_cap), kBlock, 0, s>>>(scene.xmin, scene.xmax, scene.partner, hdr,
-                                                                slots_cap);
+                                int64_t seg_cap, const SortedScene &scene, int64_t slots_cap) {
+  list_offsets_kernel<<<blocks_for(seg_cap + 1), kBlock, 0, s>>>(keys, hdr, seg_scan, seg_cap, scene, slots_cap);
   return cudaGetLastError();
 }
 

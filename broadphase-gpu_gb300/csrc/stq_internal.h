@@ -238,12 +238,11 @@ cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b);
 // device knows the count)
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n);
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms);
-// list offsets from the list-sorted keys (and the longest list)
+// list offsets from the list-sorted keys (and the longest list); the NaN
+// sentinel after every list and the padding after the last
 cudaError_t launch_list_offsets(cudaStream_t s, const unsigned long long *keys, BatchHeader *hdr, uint32_t *seg_scan,
-                                int64_t seg_cap);
+                                int64_t seg_cap, const SortedScene &scene, int64_t slots_cap);
 
-cudaError_t launch_fill_sentinels(cudaStream_t s, const SortedScene &scene, const BatchHeader *hdr,
-                                  int64_t slots_cap);
 cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const unsigned long long *keys, const uint32_t *order,
                                 const BatchHeader *hdr, int64_t rep_cap,
