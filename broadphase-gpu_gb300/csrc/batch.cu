@@ -32,17 +32,26 @@ __device__ __forceinline__ void axes_bc(int a, int &b, int &c) {
   c = a == 2 ? 1 : 2;
 }
 
-template <typename T>
-__device__ T block_sum(T v, T *red) {
+// Block sums of K values per thread with one shared-memory exchange; out[k]
+// is valid in thread 0.
+template <typename T, int K>
+__device__ void block_sums(const T (&v)[K], T (&out)[K], T (*red)[K]) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(kFullMask, v, o);
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    T x = v[k];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(kFullMask, x, o);
+    if (lane == 0) red[warp][k] = x;
+  }
   __syncthreads();
-  if (lane == 0) red[warp] = v;
-  __syncthreads();
-  T t = 0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < kBlock / 32; ++w) t += red[w];
-  return t;  // valid in thread 0
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      T t = 0;
+      for (int w = 0; w < kBlock / 32; ++w) t += red[w][k];
+      out[k] = t;
+    }
+  }
 }
 
 // ---- 0. reset the per-scene accumulators ------------------------------------------
@@ -97,11 +106,20 @@ batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
   float s1[3] = {0.f, 0.f, 0.f}, s2[3] = {0.f, 0.f, 0.f};
   uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   bool inverted = false, nan = false;
-  // warp-staged loads: 32 boxes as 11 coalesced word loads
+  // warp-staged loads: 32 boxes as 11 coalesced word loads, all issued before
+  // the first is stored (a store that waits on its load would serialise them)
   const uint32_t *src = reinterpret_cast<const uint32_t *>(boxes + t.begin);
   for (int i0 = threadIdx.x - lane; i0 < t.count; i0 += kBlock) {
     const int n = min(32, t.count - i0);
-    for (int w = lane; w < n * W; w += 32) sm[w] = src[int64_t(i0) * W + w];
+    if (n == 32) {
+      uint32_t v[W];
+#pragma unroll
+      for (int w = 0; w < W; ++w) v[w] = src[int64_t(i0) * W + w * 32 + lane];
+#pragma unroll
+      for (int w = 0; w < W; ++w) sm[w * 32 + lane] = v[w];
+    } else {
+      for (int w = lane; w < n * W; w += 32) sm[w] = src[int64_t(i0) * W + w];
+    }
     __syncwarp();
     if (lane < n) {
 #pragma unroll
@@ -118,14 +136,16 @@ batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
     }
     __syncwarp();
   }
-  __shared__ double dred[kBlock / 32];
+  __shared__ double dred[kBlock / 32][6];
   SceneRecord &r = scenes[t.scene];
+  const double mom[6] = {double(s1[0]), double(s1[1]), double(s1[2]), double(s2[0]), double(s2[1]), double(s2[2])};
+  double tot[6];
+  block_sums(mom, tot, dred);
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
     // sum(l + h) = S1 + 2 n c; sum(l^2 + h^2) = S2 + 2 c S1 + 2 n c^2
-    const double a = block_sum(double(s1[k]), dred);
-    const double q = block_sum(double(s2[k]), dred);
     if (threadIdx.x == 0) {
+      const double a = tot[k], q = tot[3 + k];
       const double ck = c[k], n = double(t.count);
       atomicAdd(&r.s1[k], a + 2.0 * n * ck);
       atomicAdd(&r.s2[k], q + 2.0 * ck * a + 2.0 * n * ck * ck);
@@ -290,21 +310,26 @@ batch_levels_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restric
     ibl[l] = inv_side(nbl[l], g.Lb);
     icl[l] = inv_side(ncl[l], g.Lc);
   }
-  unsigned long long reps[kGridLevels] = {};
+  // a thread sees at most kTileBoxes / kBlock = 16 boxes of at most 2048^2
+  // cells each: 32-bit sums per thread, 64-bit per block
+  static_assert(uint64_t(kTileBoxes / kBlock) * 2048 * 2048 < (uint64_t(1) << 32), "per-thread level sums");
+  unsigned reps[kGridLevels] = {};
   for (int i = threadIdx.x; i < t.count; i += kBlock) {
     const stq_aabb &x = boxes[t.begin + i];
 #pragma unroll
     for (int l = 0; l < kGridLevels; ++l) {
       const Range q = cell_range(x, g.axis, g.ob, ibl[l], nbl[l], g.oc, icl[l], ncl[l]);
-      reps[l] += (unsigned long long)(q.b1 - q.b0 + 1) * (unsigned long long)(q.c1 - q.c0 + 1);
+      reps[l] += unsigned(q.b1 - q.b0 + 1) * unsigned(q.c1 - q.c0 + 1);
     }
   }
-  __shared__ unsigned long long red[kBlock / 32];
+  __shared__ unsigned long long red[kBlock / 32][kGridLevels];
+  unsigned long long wide[kGridLevels], tot[kGridLevels];
 #pragma unroll
-  for (int l = 0; l < kGridLevels; ++l) {
-    const unsigned long long v = block_sum(reps[l], red);
-    if (threadIdx.x == 0) atomicAdd(&r.level_reps[l], v);
-  }
+  for (int l = 0; l < kGridLevels; ++l) wide[l] = reps[l];
+  block_sums(wide, tot, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int l = 0; l < kGridLevels; ++l) atomicAdd(&r.level_reps[l], tot[l]);
 }
 
 // ---- 4. choose the finest level within the replica budget; cell bases ----------
