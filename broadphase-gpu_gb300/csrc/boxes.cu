@@ -114,7 +114,15 @@ __device__ __forceinline__ void store_boxes(const stq_aabb &b, bool have, int64_
   }
   __syncwarp();
   uint32_t *dst = reinterpret_cast<uint32_t *>(out + base);
-  for (int i = lane; i < count * kBoxWords; i += 32) dst[i] = sm[i];
+  if (count == 32) {  // all shared-memory reads before the first store
+    uint32_t v[kBoxWords];
+#pragma unroll
+    for (int f = 0; f < kBoxWords; ++f) v[f] = sm[f * 32 + lane];
+#pragma unroll
+    for (int f = 0; f < kBoxWords; ++f) dst[f * 32 + lane] = v[f];
+  } else {
+    for (int i = lane; i < count * kBoxWords; i += 32) dst[i] = sm[i];
+  }
   __syncwarp();
 }
 
