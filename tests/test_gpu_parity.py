@@ -519,6 +519,13 @@ def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows):
         assert ctx.launches - l0 - one == 2 * min(windows, length >> 19) - 1
         assert r.status == stq.STQ_OK and r.count == len(want)
         assert np.array_equal(oracle.canonical(out), want)
+        # runs handed to the warp pass in every window, on both slots' lists
+        ctx.set_option(stq.OPT_RUN_CAP, 8)
+        out[:] = -7
+        r = ctx.broadphase_host(m, out, stq.AXIS_AUTO)
+        assert r.status == stq.STQ_OK and r.count == len(want)
+        assert np.array_equal(oracle.canonical(out), want)
+        ctx.set_option(stq.OPT_RUN_CAP, 0)
         tiny = np.empty((100, 2), np.int32)
         hb = boxes.cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
         rs = ctx.sweep_host(hb, tiny)
