@@ -38,7 +38,7 @@ constexpr size_t kOffHdr = kOffPartner + up256(sizeof(int) * kSlots);
 constexpr size_t kOffScenePairs = kOffHdr + up256(sizeof(BatchHeader));
 constexpr size_t kScratchBytes = kOffScenePairs + up256(sizeof(unsigned long long));
 
-// The scratch of every stq_sweep_static call on this device (about 4 MB).
+// The scratch of every stq_sweep_static call on this device (about 4.5 MB).
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
 // Zeroes what the sweep expects to start at zero, writes keys and indices.

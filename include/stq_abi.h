@@ -312,7 +312,7 @@ int stq_server_set_option(stq_server *server, int option, int64_t value);
  * capture), simulation steps that must stay within memory reserved up front,
  * and hosts whose own allocator forbids the CUDA runtime's. It sorts and
  * sweeps one scene (no cells) along `axis` (0, 1 or 2) on `stream` using only
- * a scratch array of about 4 MB that is static in this library: every GPU
+ * a scratch array of about 4.5 MB that is static in this library: every GPU
  * that loads the library holds it until the process exits, and it keeps the
  * last call's contents. No context, no cudaMalloc, no cudaFree.
  *   - n above STQ_STATIC_MAX_BOXES is rejected with STQ_ERR_CAPACITY before
