@@ -30,26 +30,42 @@ int64_t num_tiles(int64_t n, int tile) { return (n + tile - 1) / tile; }
 template <typename K, int BITS>
 __global__ void __launch_bounds__(kSortBlock)
 upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift,
-               uint32_t *__restrict__ hist, int64_t ntiles, const unsigned int *d_n) {
+               uint32_t *__restrict__ hist, int64_t ntiles, const unsigned int *d_n, bool match) {
   if (d_n && int64_t(*d_n) < n) n = *d_n;
   constexpr int BINS = 1 << BITS;
   constexpr int TILE = TileShape<K>::tile;
+  constexpr int ITEMS = TILE / kSortBlock;
   __shared__ uint32_t h[kSortWarps][BINS];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < kSortWarps * BINS; i += kSortBlock) (&h[0][0])[i] = 0;
   __syncthreads();
   const int64_t base = int64_t(blockIdx.x) * TILE;
-  for (int i = 0; i < TILE / kSortBlock; ++i) {
+  int d[ITEMS];  // all loads first
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
     const int64_t idx = base + int64_t(i) * kSortBlock + threadIdx.x;
-    const int d = idx < n ? int((keys[idx] >> shift) & (BINS - 1)) : BINS;
-    const unsigned peers = __match_any_sync(kFullMask, d);
-    if (d < BINS && lane == __ffs(peers) - 1) atomicAdd(&h[warp][d], __popc(peers));
+    d[i] = idx < n ? int((keys[idx] >> shift) & (BINS - 1)) : BINS;
+  }
+#pragma unroll
+  for (int i = 0; i < ITEMS; ++i) {
+    // a warp whose digits are all equal adds once; a digit that repeats
+    // within warps (the top byte of float keys: sign and exponent) is
+    // counted per distinct value; other digits by one shared atomic each
+    const int d0 = __shfl_sync(kFullMask, d[i], 0);
+    if (__all_sync(kFullMask, d[i] == d0)) {
+      if (lane == 0 && d0 < BINS) atomicAdd(&h[warp][d0], 32u);
+    } else if (match) {
+      const unsigned peers = __match_any_sync(kFullMask, d[i]);
+      if (d[i] < BINS && lane == __ffs(peers) - 1) atomicAdd(&h[warp][d[i]], __popc(peers));
+    } else if (d[i] < BINS) {
+      atomicAdd(&h[warp][d[i]], 1u);
+    }
   }
   __syncthreads();
-  for (int d = threadIdx.x; d < BINS; d += kSortBlock) {
-    uint32_t s = 0;
-    for (int w = 0; w < kSortWarps; ++w) s += h[w][d];
-    hist[int64_t(d) * ntiles + blockIdx.x] = s;
+  for (int dg = threadIdx.x; dg < BINS; dg += kSortBlock) {
+    uint32_t t = 0;
+    for (int w = 0; w < kSortWarps; ++w) t += h[w][dg];
+    hist[int64_t(dg) * ntiles + blockIdx.x] = t;
   }
 }
 
@@ -254,8 +270,10 @@ cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
   uint32_t *totals = hist + int64_t(BINS) * ntiles;
   int cur = 0;
   for (int shift = begin_bit; shift < end_bit; shift += BITS) {
+    // the top digit of 4-byte keys (float sign and exponent) repeats within warps
+    const bool match = sizeof(K) == 4 && shift + BITS >= 32;
     upsweep_kernel<K, BITS><<<unsigned(ntiles), kSortBlock, 0, s>>>(kbuf[cur], n, shift,
-                                                                     hist, ntiles, d_n);
+                                                                     hist, ntiles, d_n, match);
     scan_rows_kernel<<<BINS, kSortBlock, 0, s>>>(hist, ntiles, totals);
     scan_totals_kernel<BINS><<<1, kSortBlock, 0, s>>>(totals);
     downsweep_kernel<K, BITS, VALS><<<unsigned(ntiles), kSortBlock, 0, s>>>(
