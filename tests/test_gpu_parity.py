@@ -640,3 +640,65 @@ def test_cells_overflow_resume(ctx, stq, oracle, cuda):
     allp = np.concatenate(chunks)
     assert len(oracle.canonical(allp)) == len(allp)
     assert np.array_equal(oracle.canonical(allp), want)
+
+
+def _f32_lower_bound(C, lo, inv):
+    """Smallest float32 v with (v - lo) * inv >= C in float32 round-to-nearest
+    steps: the lower bound of cell C, found as the device finds it."""
+    def okey(f):
+        u = int(np.float32(f).view(np.uint32))
+        return (~u & 0xFFFFFFFF) if u & 0x80000000 else (u | 0x80000000)
+
+    def ofloat(k):
+        u = (k & 0x7FFFFFFF) if k & 0x80000000 else (~k & 0xFFFFFFFF)
+        return np.uint32(u).view(np.float32)
+
+    a, b = okey(-np.inf), okey(np.inf)
+    while b - a > 1:
+        m = (a + b) // 2
+        if np.float32(np.float32(ofloat(m) - lo) * inv) >= np.float32(C):
+            b = m
+        else:
+            a = m
+    return ofloat(b)
+
+
+@pytest.mark.parametrize("lo,hi,n", [(0.0, 1.0, 8), (0.1, 0.8, 7), (-0.37, 1.91, 13), (1000.25, 1003.0, 11)])
+def test_first_cell_rule_at_cell_bounds(ctx, stq, oracle, cuda, lo, hi, n):
+    """A pair found in several cells is emitted in the cell of its reference
+    point, tested on the candidate's minima against the start box's cell lower
+    bounds. Boxes whose minima sit one float below, on and one float above
+    every cell bound (computed on the host in the same float32 steps as the
+    device's grid: origin lo, n / (hi - lo) cells per unit) give the oracle's
+    pairs exactly."""
+    f32 = np.float32
+    lo, hi = f32(lo), f32(hi)
+    inv = f32(f32(n) / f32(hi - lo))
+    down = lambda v: np.nextafter(v, f32(-np.inf), dtype=np.float32)  # noqa: E731
+    up = lambda v: np.nextafter(v, f32(np.inf), dtype=np.float32)  # noqa: E731
+    cell = lambda v: int(min(max(f32(f32(v - lo) * inv), f32(0)), f32(n - 1)))  # noqa: E731
+    bounds = [_f32_lower_bound(C, lo, inv) for C in range(1, n)]
+    for C, t in enumerate(bounds, start=1):
+        assert cell(t) == C and cell(down(t)) == C - 1
+    w = f32((hi - lo) / (4 * n))  # a quarter cell: boxes reach into the next cell at most
+    rows = []
+    # the whole scene on y and z: fixes the grid's origin and extent
+    rows.append(((f32(0), lo, lo), (f32(1), hi, hi)))
+    for tb in bounds:
+        for tc in bounds[:: max(1, len(bounds) // 4)]:
+            for mb in (down(tb), tb, up(tb)):
+                for mc in (down(tc), tc, up(tc)):
+                    rows.append(((f32(0.25), mb, mc), (f32(0.75), f32(mb + w), f32(mc + w))))
+    boxes = np.zeros(len(rows), stq.AABB_DTYPE)
+    for i, (mn, mx) in enumerate(rows):
+        boxes[i]["id"] = i
+        boxes[i]["min"] = mn
+        boxes[i]["max"] = mx
+        boxes[i]["vertex_ids"] = (2 * i, 2 * i + 1, -2 * i - 1)  # edges, no shared vertex
+    want = oracle.broadphase(boxes)
+    assert len(want) > len(boxes)
+    ctx.set_option(stq.OPT_CELLS, n)
+    ctx.set_option(stq.OPT_REPLICA_BUDGET, 64)
+    got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis=0)
+    assert ctx.list_stats()["lists"] == 3 * n * n  # the grid the host computed
+    assert np.array_equal(got, want)
