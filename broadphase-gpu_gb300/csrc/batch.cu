@@ -399,19 +399,15 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
   }
 }
 
-// ---- 5. per-box replica counts (zero past the last box, up to the capacity) -----
+// ---- 5. per-box replica counts in sweep-axis order (zero past the last box, up
+// to the capacity), gathered from the counts by box index that the box-key
+// kernel wrote
 __global__ void __launch_bounds__(kBlock)
-batch_count_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict__ order,
-                   const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
+batch_count_kernel(const uint32_t *__restrict__ order, const uint32_t *__restrict__ reps,
                    const BatchHeader *hdr, uint32_t *__restrict__ counts, long long box_cap) {
   const long long N = hdr->n_boxes;
-  const int S = hdr->n_scenes;
-  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
-    const uint32_t bi = order[p];
-    const GridParams g = scenes[scene_of(box_off, S, bi)].grid;
-    const Range q = cell_range(boxes[bi], g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
-    counts[p] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
-  }
+  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock)
+    counts[p] = reps[order[p]];
   // positions past the batch contribute nothing to the scan
   for (long long i = N + blockIdx.x * (long long)kBlock + threadIdx.x; i < box_cap;
        i += (long long)gridDim.x * kBlock)
@@ -468,14 +464,18 @@ batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict
 __global__ void __launch_bounds__(kBlock)
 batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
                       const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
-                      uint32_t *__restrict__ keys, uint32_t *__restrict__ vals) {
+                      uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, uint32_t *__restrict__ reps) {
   if (int(blockIdx.x) >= hdr->n_tiles) return;
   const TileRec t = tiles[blockIdx.x];
-  const int a = scenes[t.scene].grid.axis;
+  const GridParams g = scenes[t.scene].grid;
   for (int i = threadIdx.x; i < t.count; i += kBlock) {
     const long long bi = t.begin + i;
-    keys[bi] = float_key(boxes[bi].min[a]);
+    const stq_aabb &x = boxes[bi];
+    keys[bi] = float_key(x.min[g.axis]);
     vals[bi] = uint32_t(bi);
+    // the box's replica count, by box index, while the box is read in order
+    const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
+    reps[bi] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
   }
 }
 
@@ -694,13 +694,15 @@ cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b) {
 
 cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b) {
   batch_box_keys_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr, b.box_keys,
-                                                                b.box_vals);
+                                                                b.box_vals, b.offsets);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n) {
-  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.boxes, b.order, b.box_off, b.scenes, b.hdr, b.counts,
-                                               b.box_cap);
+  // the box-key kernel left the counts by box index in the offsets buffer,
+  // which the scan of these counts overwrites afterwards
+  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.order, b.offsets, b.hdr,
+                                                                                  b.counts, b.box_cap);
   return cudaGetLastError();
 }
 
