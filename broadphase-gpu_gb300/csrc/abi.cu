@@ -192,6 +192,7 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
   b.hdr = dev_hdr(ctx);
   b.counts = ctx->counts.as<uint32_t>();
   b.offsets = ctx->offsets.as<uint32_t>();
+  b.box_cells = ctx->box_cells.as<uint2>();
   b.keys = ctx->keys64[0].as<unsigned long long>();
   b.vals = ctx->vals[0].as<uint32_t>();
   b.box_keys = ctx->bkeys[0].as<uint32_t>();
@@ -199,6 +200,7 @@ BatchBuffers batch_buffers(stq_context *ctx, const stq_aabb *boxes) {
   b.box_keys2 = ctx->bkeys[1].as<uint32_t>();
   b.box_vals2 = ctx->bvals[1].as<uint32_t>();
   b.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
+  b.sorted_keys = ctx->bkeys[ctx->order_buf].as<uint32_t>();
   b.seg_scan = ctx->seg_scan.as<uint32_t>();
   b.seg_cap = ctx->seg_cap;
   b.box_cap = ctx->box_cap;
@@ -211,6 +213,7 @@ int ensure_box_buffers(stq_context *ctx, int64_t box_cap) {
   const size_t n = size_t(std::max<int64_t>(box_cap, 1));
   STQ_CUDA(ctx, ctx->counts.ensure(sizeof(uint32_t) * n), "allocate replica counts");
   STQ_CUDA(ctx, ctx->offsets.ensure(sizeof(uint32_t) * n), "allocate replica offsets");
+  STQ_CUDA(ctx, ctx->box_cells.ensure(sizeof(uint2) * n), "allocate box cell ranges");
   STQ_CUDA(ctx, ctx->scan_ws.ensure(scan_workspace_bytes(int64_t(n))), "allocate scan workspace");
   for (int b = 0; b < 2; ++b) {
     STQ_CUDA(ctx, ctx->bkeys[b].ensure(sizeof(uint32_t) * n), "allocate box keys");
@@ -275,6 +278,7 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_box
   stage_end(ctx, kSort);
   BatchBuffers bs = b;
   bs.order = vb[ctx->order_buf];
+  bs.sorted_keys = kb[ctx->order_buf];
   stage_begin(ctx, kKeys);
   STQ_CUDA(ctx, launch_batch_counts(ctx->stream, bs, n), "launch replica counts");
   STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.counts, b.offsets, ctx->box_cap, ctx->scan_ws.ptr,
@@ -288,6 +292,7 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
                          int64_t replicas) {
   BatchBuffers bs = b;
   bs.order = ctx->bvals[ctx->order_buf].as<uint32_t>();
+  bs.sorted_keys = ctx->bkeys[ctx->order_buf].as<uint32_t>();
   STQ_CUDA(ctx, launch_batch_emit(ctx->stream, bs, n_boxes >= 0 ? n_boxes : ctx->box_cap, ctx->num_sms),
            "launch replica emit");
   stage_end(ctx, kKeys);
@@ -457,7 +462,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
     if (ctx->graph_event) cudaEventDestroy(ctx->graph_event);
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
-    for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts,
+    for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts, &ctx->box_cells,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
                       &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
                       &ctx->seg_scan, &ctx->bkeys[0], &ctx->bkeys[1],

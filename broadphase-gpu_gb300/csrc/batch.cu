@@ -400,14 +400,18 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
 }
 
 // ---- 5. per-box replica counts in sweep-axis order (zero past the last box, up
-// to the capacity), gathered from the counts by box index that the box-key
-// kernel wrote
+// to the capacity), from the cell ranges by box index that the box-key kernel
+// wrote
+__device__ __forceinline__ uint32_t cells_count(uint2 r) {
+  return ((r.x >> 11 & 2047u) - (r.x & 2047u) + 1u) * ((r.y >> 11 & 2047u) - (r.y & 2047u) + 1u);
+}
+
 __global__ void __launch_bounds__(kBlock)
-batch_count_kernel(const uint32_t *__restrict__ order, const uint32_t *__restrict__ reps,
+batch_count_kernel(const uint32_t *__restrict__ order, const uint2 *__restrict__ box_cells,
                    const BatchHeader *hdr, uint32_t *__restrict__ counts, long long box_cap) {
   const long long N = hdr->n_boxes;
   for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock)
-    counts[p] = reps[order[p]];
+    counts[p] = cells_count(box_cells[order[p]]);
   // positions past the batch contribute nothing to the scan
   for (long long i = N + blockIdx.x * (long long)kBlock + threadIdx.x; i < box_cap;
        i += (long long)gridDim.x * kBlock)
@@ -418,7 +422,8 @@ batch_count_kernel(const uint32_t *__restrict__ order, const uint32_t *__restric
 // segment is (global cell, box type): every cell holds a vertex, an edge and
 // a face list.
 __global__ void __launch_bounds__(kBlock)
-batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict__ order,
+batch_emit_kernel(const uint2 *__restrict__ box_cells, const uint32_t *__restrict__ sorted_keys,
+                  const uint32_t *__restrict__ order,
                   const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
                   const unsigned int *__restrict__ cell_base, BatchHeader *hdr,
                   const uint32_t *__restrict__ offsets, unsigned long long *__restrict__ keys,
@@ -442,16 +447,19 @@ batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict
   for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
     const uint32_t bi = order[p];
     const int sc = scene_of(box_off, S, bi);
-    const GridParams g = scenes[sc].grid;
+    const int nc = scenes[sc].grid.nc;
     const unsigned long long cb0 = cell_base[sc];
-    const stq_aabb &x = boxes[bi];
-    const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
-    const unsigned long long xk = float_key(x.min[g.axis]);
-    const unsigned long long type = type_of(x.vertex_ids[1], x.vertex_ids[2]);
+    // the box's cell range and type (8 bytes, by box index) and its sort key,
+    // instead of the 44-byte box
+    const uint2 r = box_cells[bi];
+    const int b0 = int(r.x & 2047u), b1 = int(r.x >> 11 & 2047u);
+    const int c0 = int(r.y & 2047u), c1 = int(r.y >> 11 & 2047u);
+    const unsigned long long type = r.x >> 22;
+    const unsigned long long xk = sorted_keys[p];
     uint32_t o = offsets[p];
-    for (int cb = q.b0; cb <= q.b1; ++cb)
-      for (int cc = q.c0; cc <= q.c1; ++cc) {
-        const unsigned long long seg = (cb0 + (unsigned long long)(cb * g.nc + cc)) * 3ull + type;
+    for (int cb = b0; cb <= b1; ++cb)
+      for (int cc = c0; cc <= c1; ++cc) {
+        const unsigned long long seg = (cb0 + (unsigned long long)(cb * nc + cc)) * 3ull + type;
         keys[o] = (seg << 32) | xk;
         vals[o] = bi;
         ++o;
@@ -464,7 +472,7 @@ batch_emit_kernel(const stq_aabb *__restrict__ boxes, const uint32_t *__restrict
 __global__ void __launch_bounds__(kBlock)
 batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
                       const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
-                      uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, uint32_t *__restrict__ reps) {
+                      uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, uint2 *__restrict__ box_cells) {
   if (int(blockIdx.x) >= hdr->n_tiles) return;
   const TileRec t = tiles[blockIdx.x];
   const GridParams g = scenes[t.scene].grid;
@@ -473,9 +481,12 @@ batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restr
     const stq_aabb &x = boxes[bi];
     keys[bi] = float_key(x.min[g.axis]);
     vals[bi] = uint32_t(bi);
-    // the box's replica count, by box index, while the box is read in order
+    // the box's cell range and type, by box index, while the box is read in
+    // order (cell coordinates are below 2048: 11 bits)
     const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
-    reps[bi] = uint32_t(q.b1 - q.b0 + 1) * uint32_t(q.c1 - q.c0 + 1);
+    const unsigned type = unsigned(type_of(x.vertex_ids[1], x.vertex_ids[2]));
+    box_cells[bi] = make_uint2(unsigned(q.b0) | unsigned(q.b1) << 11 | type << 22,
+                               unsigned(q.c0) | unsigned(q.c1) << 11);
   }
 }
 
@@ -694,20 +705,19 @@ cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b) {
 
 cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b) {
   batch_box_keys_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr, b.box_keys,
-                                                                b.box_vals, b.offsets);
+                                                                b.box_vals, b.box_cells);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n) {
-  // the box-key kernel left the counts by box index in the offsets buffer,
-  // which the scan of these counts overwrites afterwards
-  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.order, b.offsets, b.hdr,
+  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.order, b.box_cells, b.hdr,
                                                                                   b.counts, b.box_cap);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms) {
-  batch_emit_kernel<<<blocks_for(n), kBlock, 0, s>>>(b.boxes, b.order, b.box_off, b.scenes, b.cell_base, b.hdr,
+  batch_emit_kernel<<<blocks_for(n), kBlock, 0, s>>>(b.box_cells, b.sorted_keys, b.order, b.box_off, b.scenes,
+                                                     b.cell_base, b.hdr,
                                               b.offsets, b.keys, b.vals, b.rep_cap, b.seg_cap);
   return cudaGetLastError();
 }

@@ -219,9 +219,12 @@ struct BatchBuffers {
   unsigned int *cell_base;      // n_scenes + 1
   BatchHeader *hdr;
   uint32_t *counts, *offsets;   // per box position in sweep-axis order
+  uint2 *box_cells;             // per box index: cell range and type
+                                // (b0 | b1 << 11 | type << 22, c0 | c1 << 11)
   uint32_t *box_keys, *box_vals;  // box sort input (key, box index), double-buffered with
   uint32_t *box_keys2, *box_vals2;
   const uint32_t *order;        // boxes in sweep-axis order (box sort output)
+  const uint32_t *sorted_keys;  // their sort keys (sweep-axis minimum images)
   unsigned long long *keys;     // replica keys (sort input)
   uint32_t *vals;               // replica box indices (sort input)
   uint32_t *seg_scan;           // first sorted replica of each segment (cell x type),
