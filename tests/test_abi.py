@@ -37,6 +37,29 @@ def test_python_binding_covers_header(stq):
     assert declared_functions() <= set(stq.ABI_SIGNATURES)
 
 
+def header_enums(prefix):
+    """NAME -> value of the enumerators of include/stq_abi.h that start with prefix."""
+    text = re.sub(r"/\*.*?\*/", "", (INCLUDE / "stq_abi.h").read_text(), flags=re.S)
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(" + prefix + r"[A-Z0-9_]+)\s*=\s*(-?\d+)", text)}
+
+
+def test_python_constants_match_header(stq):
+    """The binding's option, axis and status numbers are the header's."""
+    opts = header_enums("STQ_OPT_")
+    assert len(opts) >= 12
+    for name, value in opts.items():
+        assert getattr(stq, OPT_ALIASES.get(name, name[len("STQ_"):])) == value, name
+    for name, value in header_enums("STQ_ERR_").items():
+        assert getattr(stq, name) == value, name
+    for name, value in header_enums("STQ_AXIS_").items():
+        assert getattr(stq, name[len("STQ_"):]) == value, name
+
+
+# binding names that shorten the header's
+OPT_ALIASES = {"STQ_OPT_LANES_PER_ENTRY": "OPT_LANES", "STQ_OPT_QUEUE_DEPTH": "OPT_QUEUE",
+               "STQ_OPT_BLOCK_SIZE": "OPT_BLOCK", "STQ_OPT_CANDIDATES_PER_LANE": "OPT_PER_LANE"}
+
+
 def test_box_layout_matches_reference(stq, tmp_path):
     dt = stq.AABB_DTYPE
     assert dt.itemsize == 44
