@@ -284,7 +284,7 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_box
   STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.counts, b.offsets, ctx->box_cap, ctx->scan_ws.ptr,
                                    &b.hdr->replicas, &ctx->launches),
            "launch replica scan");
-  ctx->launches += 6;
+  ctx->launches += 7;  // reset, statistics, policy, levels, choose, box keys, counts
   return STQ_OK;
 }
 
@@ -402,7 +402,8 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   if (timed) stage_begin(ctx, count_mode ? kCountSweep : kSweep);
   STQ_CUDA(ctx, launch_sweep(s, p, ctx->tuning, count_mode, ctx->num_sms), "launch sweep");
   if (timed) stage_end(ctx, count_mode ? kCountSweep : kSweep);
-  ctx->launches += 1;
+  // the sweep, and the warp pass over handed-over runs when there is a run cap
+  ctx->launches += p.end > p.begin ? (p.run_cap ? 2 : 1) : 0;
   return STQ_OK;
 }
 

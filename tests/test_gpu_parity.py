@@ -473,8 +473,8 @@ def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, over
         ctx.set_option(stq.OPT_HOST_OVERLAP, overlap)
         windows = min(ctx.get_option(stq.OPT_HOST_WINDOWS), length >> 19)
         assert windows == min(16, length >> 19)
-        # per window: a sweep and the kernel that publishes its pair count
-        assert launches - other == (2 * windows - 1 if overlap == 1 else 1 - 2 * windows)
+        # per window: a sweep, its warp pass and the kernel that publishes its pair count
+        assert launches - other == (3 * windows - 2 if overlap == 1 else 2 - 3 * windows)
         hb = boxes.cpu().numpy().view(stq.AABB_DTYPE).reshape(-1)
         r = ctx.sweep_host(hb, out)
         assert r.status == stq.STQ_OK and np.array_equal(oracle.canonical(out[: r.count]), want)
@@ -516,7 +516,7 @@ def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows):
         out[:] = -7
         l0 = ctx.launches
         r = ctx.broadphase_host(m, out, stq.AXIS_AUTO)
-        assert ctx.launches - l0 - one == 2 * min(windows, length >> 19) - 1
+        assert ctx.launches - l0 - one == 3 * min(windows, length >> 19) - 2
         assert r.status == stq.STQ_OK and r.count == len(want)
         assert np.array_equal(oracle.canonical(out), want)
         # runs handed to the warp pass in every window, on both slots' lists
