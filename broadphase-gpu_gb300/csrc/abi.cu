@@ -519,7 +519,8 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
       if (value != 0 && value != 4 && value != 8) return fail(ctx, STQ_ERR_INVALID_ARG, "radix bits: 4 or 8");
       break;
     case STQ_OPT_CELLS:
-      if (value > 2048) return fail(ctx, STQ_ERR_INVALID_ARG, "cells: 0 (auto), 1 (off) or a grid side <= 2048");
+      if (value > kMaxGridSide)
+        return fail(ctx, STQ_ERR_INVALID_ARG, "cells: 0 (auto), 1 (off) or a grid side <= 2048");
       break;
     case STQ_OPT_CELL_SCALE:
       if (value > 64) return fail(ctx, STQ_ERR_INVALID_ARG, "cell scale: 1..64");

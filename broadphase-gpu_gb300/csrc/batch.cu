@@ -164,7 +164,7 @@ batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
 __device__ int grid_side(float L, float h) {
   if (!(L > 0.f) || !(h > 0.f) || !isfinite(L)) return 1;
   const float s = ceilf(L / h);
-  return s > 2048.f ? 2048 : (s < 1.f ? 1 : int(s));
+  return s > float(kMaxGridSide) ? kMaxGridSide : (s < 1.f ? 1 : int(s));
 }
 
 __device__ __forceinline__ int level_side(int base, int level) {
@@ -312,7 +312,8 @@ batch_levels_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restric
   }
   // a thread sees at most kTileBoxes / kBlock = 16 boxes of at most 2048^2
   // cells each: 32-bit sums per thread, 64-bit per block
-  static_assert(uint64_t(kTileBoxes / kBlock) * 2048 * 2048 < (uint64_t(1) << 32), "per-thread level sums");
+  static_assert(uint64_t(kTileBoxes / kBlock) * kMaxGridSide * kMaxGridSide < (uint64_t(1) << 32),
+                "per-thread level sums");
   unsigned reps[kGridLevels] = {};
   for (int i = threadIdx.x; i < t.count; i += kBlock) {
     const stq_aabb &x = boxes[t.begin + i];
@@ -482,7 +483,8 @@ batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restr
     keys[bi] = float_key(x.min[g.axis]);
     vals[bi] = uint32_t(bi);
     // the box's cell range and type, by box index, while the box is read in
-    // order (cell coordinates are below 2048: 11 bits)
+    // order (cell coordinates are below kMaxGridSide: 11 bits)
+    static_assert(kMaxGridSide <= 2048, "11-bit cell coordinates");
     const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
     const unsigned type = unsigned(type_of(x.vertex_ids[1], x.vertex_ids[2]));
     box_cells[bi] = make_uint2(unsigned(q.b0) | unsigned(q.b1) << 11 | type << 22,

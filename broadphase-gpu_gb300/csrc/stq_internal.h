@@ -51,6 +51,10 @@ enum : int {
   kFlagReplicaOverflow = 4,  // cell replicas exceed the replica buffers
 };
 
+// Cells per axis of a scene's grid at most (automatic or STQ_OPT_CELLS); cell
+// coordinates then fit 11 bits, as the per-box cell records pack them.
+constexpr int kMaxGridSide = 2048;
+
 // Cell grid on the two non-sweep axes b, c (the other two axes in increasing
 // order). A box is replicated into every cell its [min, max] range touches;
 // cell coordinates are a monotone function of the bound, so a pair that
