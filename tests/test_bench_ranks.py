@@ -48,3 +48,34 @@ def test_single_process_passes_values_through():
 
     assert bench.max_over_ranks(None, 1.5, "cpu") == 1.5
     assert bench.job_rate(10, 1, 2.0) == 5.0
+
+
+def test_clock_summary_keeps_the_timed_region_and_names_throttle_reasons():
+    """The clock record the JSON line carries: median SM clock and maximum over
+    the samples inside the timed region, and the throttle reasons seen there."""
+    import datetime
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    t0 = datetime.datetime(2026, 1, 2, 3, 4, 5)
+    rows = []
+    for i, (mhz, reasons) in enumerate([(1500, "Not Active,Not Active,Not Active,Not Active"),
+                                        (2070, "Not Active,Not Active,Not Active,Active"),
+                                        (2070, "Not Active,Not Active,Not Active,Not Active"),
+                                        (2055, "Active,Not Active,Not Active,Not Active"),
+                                        (900, "Not Active,Not Active,Not Active,Not Active")]):
+        ts = (t0 + datetime.timedelta(milliseconds=100 * i)).strftime("%Y/%m/%d %H:%M:%S.%f")[:-3]
+        rows.append(f"{ts}, 0, {mhz}, 2070, 900.0, 0x0, {reasons}")
+    s = bench.ClockSampler(0)
+    s.out = "\n".join(rows)
+    base = t0.timestamp()
+    s.mark(base + 0.1, base + 0.3)  # samples 1..3
+    c = s.summary()
+    assert c["samples"] == 3 and c["sm_mhz"] == 2070 and c["sm_max_mhz"] == 2070
+    assert c["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    s.mark(base + 0.41, base + 0.42)  # shorter than the period: the nearest sample
+    c = s.summary()
+    assert c["samples"] == 1 and c["sm_mhz"] == 900 and c["reasons"] == []
+    s.out = ""
+    assert bench.ClockSampler(0).summary()["reasons"] == ["unavailable"]
