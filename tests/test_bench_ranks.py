@@ -79,3 +79,18 @@ def test_clock_summary_keeps_the_timed_region_and_names_throttle_reasons():
     assert c["samples"] == 1 and c["sm_mhz"] == 900 and c["reasons"] == []
     s.out = ""
     assert bench.ClockSampler(0).summary()["reasons"] == ["unavailable"]
+
+
+def test_committed_profiles_feed_the_bench_line():
+    """The roofline's traffic comes from the committed ncu figures, and every
+    profile summary states the ncu command that made it (clocks left alone)."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    t = bench.ncu_traffic("sweep", "crumpled16x250")
+    assert isinstance(t, int) and t > 977_114_680  # at least the algorithmic bytes
+    summaries = sorted((ROOT / "profiles").glob("*.md"))
+    assert len(summaries) >= 3
+    for p in summaries:
+        text = p.read_text()
+        assert "ncu " in text and "--clock-control none" in text, p.name
