@@ -1,13 +1,15 @@
 // static_sweep.cu - the one entry point that allocates nothing.
 //
 // Some callers cannot allocate device memory at the moment they need a broad
-// phase: code recorded into a CUDA graph by stream capture (cudaMalloc is not
-// a stream operation and breaks the capture), simulation steps that run under
-// a fixed memory budget reserved up front, or hosts whose allocator forbids
-// the CUDA runtime's. stq_sweep_static serves them: it sorts and sweeps one
-// scene of at most STQ_STATIC_MAX_BOXES boxes using only the file-scope
-// scratch array below, which every GPU that loads this library holds until
-// the process exits. The caller passes the boxes and the pair buffer.
+// phase: simulation steps that run under a memory budget reserved up front
+// (an out-of-memory error in the middle of a step is not recoverable for
+// them), hosts whose own pooling allocator owns the device memory and forbids
+// the CUDA runtime's, and real-time loops that cannot take the device-wide
+// synchronisation cudaFree may cause. stq_sweep_static serves them: it sorts
+// and sweeps one scene of at most STQ_STATIC_MAX_BOXES boxes using only the
+// file-scope scratch array below, which every GPU that loads this library
+// holds until the process exits. The caller passes the boxes and the pair
+// buffer.
 #include <mutex>
 
 #include "stq_device.cuh"
@@ -41,7 +43,9 @@ constexpr size_t kScratchBytes = kOffScenePairs + up256(sizeof(unsigned long lon
 // The scratch of every stq_sweep_static call on this device (about 4.5 MB).
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
-// Zeroes what the sweep expects to start at zero, writes keys and indices.
+// Writes the scene's sizes into the header (zeroed by the host before this
+// launch, so the NaN flag that any block may set is never cleared after it),
+// the sort keys and the box indices.
 __global__ void static_keys_kernel(const stq_aabb *__restrict__ boxes, int n, int axis,
                                    unsigned char *scratch) {
   BatchHeader *hdr = reinterpret_cast<BatchHeader *>(scratch + kOffHdr);
@@ -51,13 +55,9 @@ __global__ void static_keys_kernel(const stq_aabb *__restrict__ boxes, int n, in
   if (i == 0) {
     hdr->n_boxes = n;
     hdr->n_scenes = 1;
-    hdr->flags = 0;
     hdr->replicas = unsigned(n);
     hdr->cells = 1;
     hdr->length = unsigned(n);
-    hdr->work = 0;
-    hdr->pairs = 0;
-    *reinterpret_cast<unsigned long long *>(scratch + kOffScenePairs) = 0;
   }
   bool nan = false;
   if (i < n) {
@@ -130,6 +130,9 @@ extern "C" int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, st
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int ni = int(n);
   const int blocks = (ni + 1 + int(kSortedPad) + 255) / 256;
+  // the header and the scene's pair counter start at zero (the array keeps
+  // the last call's contents); a memset on the stream, not an allocation
+  if (cudaMemsetAsync(scratch + kOffHdr, 0, kScratchBytes - kOffHdr, s) != cudaSuccess) return STQ_ERR_CUDA;
   static_keys_kernel<<<(ni + 255) / 256 > 0 ? (ni + 255) / 256 : 1, 256, 0, s>>>(d_boxes, ni, axis,
                                                                                    scratch);
   uint32_t *kb[2] = {reinterpret_cast<uint32_t *>(scratch + kOffKeys0),

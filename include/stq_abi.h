@@ -307,23 +307,26 @@ int stq_server_set_option(stq_server *server, int option, int64_t value);
 
 /* ---- sweep without any allocation -----------------------------------------
  * No counterpart in the reference. For callers that cannot allocate device
- * memory when they need a broad phase: work recorded into a CUDA graph by
- * stream capture (cudaMalloc is not a stream operation and invalidates the
- * capture), simulation steps that must stay within memory reserved up front,
- * and hosts whose own allocator forbids the CUDA runtime's. It sorts and
- * sweeps one scene (no cells) along `axis` (0, 1 or 2) on `stream` using only
- * a scratch array of about 4.5 MB that is static in this library: every GPU
- * that loads the library holds it until the process exits, and it keeps the
- * last call's contents. No context, no cudaMalloc, no cudaFree.
+ * memory when they need a broad phase: simulation steps that must stay within
+ * memory reserved up front (an out-of-memory error in mid-step is not
+ * recoverable for them), hosts whose own pooling allocator owns the device
+ * memory and forbids the CUDA runtime's, and real-time loops that cannot take
+ * the device-wide synchronisation cudaFree may cause. It sorts and sweeps one
+ * scene (no cells) along `axis` (0, 1 or 2) on `stream` using only a scratch
+ * array of about 4.5 MB that is static in this library: every GPU that loads
+ * the library holds it until the process exits, and it keeps the last call's
+ * contents (each call clears what must start at zero). No context, no
+ * cudaMalloc, no cudaFree.
  *   - n above STQ_STATIC_MAX_BOXES is rejected with STQ_ERR_CAPACITY before
  *     any GPU work (use stq_sweep for larger scenes);
  *   - the first call on a device looks up the scratch array's device address
  *     (with that device current); make that first call before any stream
- *     capture that should contain later calls;
+ *     capture begins;
  *   - all calls on a device share the array: calls that overlap on the GPU
  *     (other streams, other host threads) race and must be serialised;
  *   - pairs as stq_sweep; *count = pairs written, *total (may be NULL) = pairs
- *     found; STQ_OVERFLOW if they did not all fit (no resume cursor).
+ *     found; STQ_OVERFLOW if they did not all fit (no resume cursor);
+ *     STQ_ERR_INVALID_INPUT if a bound is NaN.
  * The call synchronises `stream` before returning. */
 #define STQ_STATIC_MAX_BOXES 65536
 int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, stq_pair *d_pairs,

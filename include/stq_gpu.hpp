@@ -17,9 +17,15 @@
 // leaving room for the narrow phase, and on overflow grows it or halves
 // MAX_OVERLAP_CUTOFF and sweeps again; tidstart is the resume cursor.
 // Differences: pairs are (smaller id, larger id); errors throw
-// stq::gpu::Error instead of calling exit(); tidstart counts positions of the
-// prepared sweep order (stq_prepared_length: replicas of boxes in cells, in
-// vertex, edge and face lists); devcount is ignored (one GPU).
+// stq::gpu::Error instead of calling exit(); devcount is ignored (one GPU).
+// tidstart and MAX_OVERLAP_CUTOFF count start boxes as in the reference; the
+// library's sweep order holds a box once per cell it touches, and a range of
+// start boxes maps to a proportional range of those positions
+// (start_position below).
+//
+// Compile-time option: STQ_GPU_MAX_OVERLAP_SIZE caps the pair buffer at that
+// many pairs, as a device with less free memory would (to exercise the
+// overflow-and-resume path on small scenes).
 #pragma once
 
 #include <cuda_runtime.h>
@@ -88,7 +94,12 @@ struct MemHandler {
   // src/memory.cuh:163-167
   size_t __getLargestOverlap() {
     const size_t a = __getAllocatable();
-    return a > kCCDConfigBytes ? (a - kCCDConfigBytes) / (kCCDDataBytes + 3 * sizeof(int2)) : 0;
+    const size_t n = a > kCCDConfigBytes ? (a - kCCDConfigBytes) / (kCCDDataBytes + 3 * sizeof(int2)) : 0;
+#ifdef STQ_GPU_MAX_OVERLAP_SIZE
+    return std::min<size_t>(n, size_t(STQ_GPU_MAX_OVERLAP_SIZE));
+#else
+    return n;
+#endif
   }
   void setOverlapSize() { MAX_OVERLAP_SIZE = __getLargestOverlap(); }
   // src/memory.cuh:171-188
@@ -167,7 +178,26 @@ void constructBoxes(const MatD &vertices_t0, const MatD &vertices_t1, const MatI
   for (size_t i = offset; i < boxes.size(); ++i) boxes[i].id += int(offset);
 }
 
+// First sweep position of start box t (t in [0, N]) of a prepared scene with
+// `length` positions: positions [pos(t0), pos(t1)) are the share of start
+// boxes [t0, t1). pos(0) = 0, pos(N) = length, monotone, and since a scene has
+// at least N positions (every box has at least one replica) every start box
+// gets at least one position. The cursor and cutoff of run_sweep_sharedqueue
+// count start boxes, as the reference's do, through this map.
+inline int64_t start_position(int64_t t, int64_t N, int64_t length) {
+  if (N <= 0 || t >= N) return length;
+  return t <= 0 ? 0 : t * length / N;
+}
+
 // STQ sweep of host boxes; pairs stay on the device in d_overlaps[0..*d_count).
+// One call sweeps start boxes [tidstart, tidstart + MAX_OVERLAP_CUTOFF) and
+// advances tidstart by the cutoff (src/simulation.cu:747), so a single call
+// with the default cutoff N sweeps the whole scene (app/main.cu:140-143), and
+// a caller that loops `while (tidstart < N)` gets every pair exactly once. On
+// overflow the call reruns its range with the buffer grown, or with the cutoff
+// halved (src/memory.cuh:171-188), as the reference's loop does
+// (src/simulation.cu:714-745). The sweep axis is x, as in the reference
+// (src/simulation.cu:637), so every resumed call sees the same sorted order.
 inline void run_sweep_sharedqueue(const Aabb *boxes, MemHandler *memhandle, int N, int nbox,
                                   std::vector<std::pair<int, int>> &finOverlaps,
                                   int2 *&d_overlaps, int *&d_count, int &threads, int &tidstart,
@@ -180,19 +210,26 @@ inline void run_sweep_sharedqueue(const Aabb *boxes, MemHandler *memhandle, int 
   stq_context *ctx = detail::context();
   {
     detail::DeviceArray<stq_aabb> dB(reinterpret_cast<const stq_aabb *>(boxes), size_t(N));
-    detail::check(stq_prepare(ctx, dB.p, N, STQ_AXIS_AUTO), ctx);
+    detail::check(stq_prepare(ctx, dB.p, N, STQ_AXIS_X), ctx);
   }
+  const int64_t length = stq_prepared_length(ctx);
   memhandle->setOverlapSize();
   detail::cuda(cudaMalloc(&d_count, sizeof(int)), "cudaMalloc");
   int64_t count = 0, next = 0, total = 0;
   while (true) {
     detail::cuda(cudaMalloc(&d_overlaps, sizeof(int2) * std::max<size_t>(1, memhandle->MAX_OVERLAP_SIZE)),
                  "cudaMalloc");
-    const int st = stq_sweep_prepared(ctx, tidstart, int64_t(memhandle->MAX_OVERLAP_CUTOFF),
-                                      reinterpret_cast<stq_pair *>(d_overlaps),
+    const int64_t t1 = std::min<int64_t>(int64_t(N), int64_t(tidstart) + int64_t(memhandle->MAX_OVERLAP_CUTOFF));
+    const int64_t p0 = start_position(tidstart, N, length), p1 = start_position(t1, N, length);
+    if (p1 <= p0) {  // nothing left to sweep
+      count = 0;
+      break;
+    }
+    const int st = stq_sweep_prepared(ctx, p0, p1 - p0, reinterpret_cast<stq_pair *>(d_overlaps),
                                       int64_t(memhandle->MAX_OVERLAP_SIZE), &count, &next, &total);
     if (st == STQ_OK) break;
     if (st != STQ_OVERFLOW && st != STQ_ERR_CAPACITY) detail::check(st, ctx);
+    // the partial result is dropped: the range is swept again whole
     cudaFree(d_overlaps);
     d_overlaps = nullptr;
     const size_t before = memhandle->MAX_OVERLAP_SIZE, cut = memhandle->MAX_OVERLAP_CUTOFF;
@@ -201,7 +238,7 @@ inline void run_sweep_sharedqueue(const Aabb *boxes, MemHandler *memhandle, int 
       throw Error(STQ_ERR_NO_MEMORY, "pair buffer cannot grow and the cutoff cannot shrink");
   }
   memhandle->realcount = int(count);
-  tidstart = int(next);
+  tidstart = int(std::min<int64_t>(int64_t(tidstart) + int64_t(memhandle->MAX_OVERLAP_CUTOFF), INT32_MAX));
   const int c = int(count);
   detail::cuda(cudaMemcpy(d_count, &c, sizeof(int), cudaMemcpyHostToDevice), "cudaMemcpy");
 #ifdef KEEP_CPU_OVERLAPS

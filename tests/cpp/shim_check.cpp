@@ -3,8 +3,14 @@
 // KEEP_CPU_OVERLAPS, then run_sweep_multigpu. Reads a mesh from a binary file
 // and writes the boxes and both pair lists for the test to compare.
 //
-//   shim_check <mesh.bin> <out_prefix> [memlimit_gb]
+//   shim_check <mesh.bin> <out_prefix> once|loop [memlimit_gb]
 //   mesh.bin: int64 nV, nE, nF; f64 V0[nV*3]; f64 V1[nV*3]; i32 E[nE*2]; i32 F[nF*3]
+//
+// once: a single run_sweep_sharedqueue call, exactly as app/main.cu:140-143
+//       makes it; tidstart must come back >= N.
+// loop: calls while (tidstart < N), freeing the previous call's buffers
+//       (built with STQ_GPU_MAX_OVERLAP_SIZE so that the pair buffer overflows
+//       and the cutoff is halved).
 #define KEEP_CPU_OVERLAPS
 #include "stq_gpu.hpp"
 
@@ -43,7 +49,9 @@ int main(int argc, char **argv) {
   read(in, F, n[2], 3);
   if (!in) return 3;
   const std::string out = argv[2];
-  const int memlimit = argc > 3 ? std::atoi(argv[3]) : 0;
+  const std::string mode = argc > 3 ? argv[3] : "once";
+  const int memlimit = argc > 4 ? std::atoi(argv[4]) : 0;
+  if (mode != "once" && mode != "loop") return 2;
   try {
     std::vector<stq::gpu::Aabb> boxes;
     stq::gpu::constructBoxes(V0, V1, E, F, boxes);
@@ -57,19 +65,19 @@ int main(int argc, char **argv) {
     int *d_count = nullptr;
     int threads = 0, tidstart = 0, devcount = 1;
     const int N = int(boxes.size());
-    // resume over start positions until the whole scene is swept
-    const int64_t length = [&] {
-      stq::gpu::run_sweep_sharedqueue(boxes.data(), memhandle, N, 0, overlaps, d_overlaps, d_count,
-                                      threads, tidstart, devcount, memlimit);
-      return stq_prepared_length(stq::gpu::detail::context());
-    }();
+    stq::gpu::run_sweep_sharedqueue(boxes.data(), memhandle, N, 0, overlaps, d_overlaps, d_count,
+                                    threads, tidstart, devcount, memlimit);
     int calls = 1;
-    while (tidstart < length) {
+    while (mode == "loop" && tidstart < N) {
       cudaFree(d_overlaps);
       cudaFree(d_count);
       stq::gpu::run_sweep_sharedqueue(boxes.data(), memhandle, N, 0, overlaps, d_overlaps, d_count,
                                       threads, tidstart, devcount, memlimit);
       ++calls;
+    }
+    if (tidstart < N) {
+      std::fprintf(stderr, "error: tidstart %d < N %d after %d call(s)\n", tidstart, N, calls);
+      return 4;
     }
     int dc = -1;
     cudaMemcpy(&dc, d_count, sizeof(int), cudaMemcpyDeviceToHost);
@@ -83,8 +91,8 @@ int main(int argc, char **argv) {
       std::ofstream f(out + ".plain", std::ios::binary);
       for (auto &p : plain) f.write(reinterpret_cast<const char *>(&p), sizeof p);
     }
-    std::printf("boxes %d stq_pairs %zu plain_pairs %zu calls %d cutoff %zu last_count %d\n", N,
-                overlaps.size(), plain.size(), calls, memhandle->MAX_OVERLAP_CUTOFF, dc);
+    std::printf("boxes %d stq_pairs %zu plain_pairs %zu calls %d cutoff %zu last_count %d tidstart %d\n", N,
+                overlaps.size(), plain.size(), calls, memhandle->MAX_OVERLAP_CUTOFF, dc, tidstart);
     cudaFree(d_overlaps);
     cudaFree(d_count);
     delete memhandle;

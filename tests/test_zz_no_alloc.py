@@ -15,8 +15,8 @@ def call_static(stq, boxes_dev, n, axis, pairs, cap, stream):
     lib = stq.load_library()
     count, total = ctypes.c_int64(), ctypes.c_int64()
     st = lib.stq_sweep_static(ctypes.c_void_p(boxes_dev.data_ptr() if boxes_dev is not None else 0), n,
-                              axis, ctypes.c_void_p(pairs.data_ptr()), cap, ctypes.byref(count),
-                              ctypes.byref(total), ctypes.c_void_p(stream))
+                              axis, ctypes.c_void_p(pairs.data_ptr() if pairs is not None else 0), cap,
+                              ctypes.byref(count), ctypes.byref(total), ctypes.c_void_p(stream))
     return st, count.value, total.value
 
 
@@ -61,3 +61,32 @@ def test_static_sweep_matches_stq_sweep_twice_in_a_row(stq, oracle, cuda):
         d = torch.from_numpy(scenes[0].view(np.int32).reshape(-1, 11).copy()).to(cuda)
         st, count, total = call_static(stq, d, len(scenes[0]), 0, pa, 100, stream)
         assert st == stq.STQ_OVERFLOW and count == 100 and total > 100
+
+
+@pytest.mark.gpu
+def test_static_sweep_edge_cases(stq, oracle, cuda):
+    """Empty and one-box scenes, a zero-capacity buffer (the true total is still
+    reported), and a NaN bound far from the first block: the error is reported
+    and the next clean call is not affected by it."""
+    import torch
+
+    stream = torch.cuda.current_stream(cuda).cuda_stream
+    pa = torch.empty((1 << 20, 2), dtype=torch.int32, device=cuda)
+    b = stq.random_boxes(20000, sliver_frac=0.05, seed=23)
+    c = 0.5 * (b["min"] + b["max"])
+    b["min"], b["max"] = c - 0.01, c + 0.01
+    d = torch.from_numpy(b.view(np.int32).reshape(-1, 11).copy()).to(cuda)
+    want = oracle.broadphase(b)
+    assert len(want) > 1000
+    assert call_static(stq, None, 0, 0, pa, 1 << 20, stream) == (stq.STQ_OK, 0, 0)
+    assert call_static(stq, d, 1, 1, pa, 1 << 20, stream) == (stq.STQ_OK, 0, 0)
+    st, count, total = call_static(stq, d, len(b), 0, None, 0, stream)
+    assert (st, count, total) == (stq.STQ_OVERFLOW, 0, len(want))
+    bad = b.copy()
+    bad["min"][15000, 1] = np.nan  # in block 58 of the key pass, not block 0
+    dbad = torch.from_numpy(bad.view(np.int32).reshape(-1, 11).copy()).to(cuda)
+    st, _, _ = call_static(stq, dbad, len(bad), 0, pa, 1 << 20, stream)
+    assert st == stq.STQ_ERR_INVALID_INPUT
+    st, count, total = call_static(stq, d, len(b), 0, pa, 1 << 20, stream)
+    assert st == stq.STQ_OK and count == total == len(want)
+    assert np.array_equal(oracle.canonical(pa[:count].cpu().numpy()), want)
