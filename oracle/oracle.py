@@ -1,9 +1,15 @@
 """ctypes binding of the CPU oracle (oracle/stq_oracle.cpp). TEST INFRASTRUCTURE.
 
 Only the tests, the smoke check and the benchmark's CPU-baseline and reference
-legs use this module, to check and time against. Parity status: unpinned by reference golden vectors
-(the reference ships none and its CPU library cannot be built here); pinned
-by the hand-derived known-answer cases under tests/golden/.
+legs use this module, to check and time against.
+
+Parity status: pinned to the reference's own code. Where the reference's
+source tree is present, `make ref` compiles its src/cpu/aabb.cpp and
+src/cpu/sweep.cpp unchanged (against the stand-in headers of ref_shim/) into
+_ref/libstq_ref.so; the tests check the restatement against it (ref_* below),
+and tests/golden/make_ref_golden.py writes its outputs as golden vectors that
+travel with the repository. The hand-derived known-answer cases under
+tests/golden/ pin the corner cases on top.
 """
 from __future__ import annotations
 
@@ -15,6 +21,8 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "libstq_oracle.so"
+REF_LIB = HERE / "_ref" / "libstq_ref.so"
+REF_TREE = Path("/root/reference")  # the reference's sources, where present
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
@@ -122,3 +130,59 @@ def time_sample(boxes: np.ndarray, stride: int, threads: int = 0) -> tuple[float
 
 def default_threads() -> int:
     return int(lib().oracle_default_threads())
+
+
+# ---- the reference's own CPU code (oracle/_ref), where it could be built ------
+_ref = None
+
+
+def build_ref() -> bool:
+    """Compiles oracle/_ref/libstq_ref.so from the reference's source tree, if
+    that tree is present; returns whether the library exists."""
+    if (REF_TREE / "src" / "cpu" / "sweep.cpp").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REF_TREE}"], check=True)
+    return REF_LIB.exists()
+
+
+def ref_available() -> bool:
+    return REF_LIB.exists()
+
+
+def ref_lib() -> ctypes.CDLL:
+    global _ref
+    if _ref is None:
+        L = ctypes.CDLL(str(REF_LIB))
+        L.ref_construct_boxes.argtypes = [_vp, _vp, _i64, _vp, _i64, _vp, _i64, ctypes.c_double, ctypes.c_int, _vp]
+        L.ref_construct_boxes.restype = None
+        L.ref_broadphase.argtypes = [_vp, _i64, ctypes.c_int, ctypes.POINTER(_vp)]
+        L.ref_broadphase.restype = _i64
+        L.ref_free.argtypes = [_vp]
+        _ref = L
+    return _ref
+
+
+def ref_construct_boxes(V0, V1, E, F, aabb_dtype, inflation_radius: float = 0.0, threads: int = 0) -> np.ndarray:
+    """stq::cpu::constructBoxes of the reference itself (src/cpu/aabb.cpp:7-95)."""
+    V0 = np.ascontiguousarray(V0, np.float64)
+    V1 = np.ascontiguousarray(V1, np.float64)
+    E = np.ascontiguousarray(E, np.int32).reshape(-1, 2)
+    F = np.ascontiguousarray(F, np.int32).reshape(-1, 3)
+    out = np.empty(V0.shape[0] + E.shape[0] + F.shape[0], aabb_dtype)
+    ref_lib().ref_construct_boxes(V0.ctypes.data, V1.ctypes.data, V0.shape[0], E.ctypes.data, E.shape[0],
+                                  F.ctypes.data, F.shape[0], inflation_radius, threads, out.ctypes.data)
+    return out
+
+
+def ref_broadphase(boxes: np.ndarray, threads: int = 0) -> np.ndarray:
+    """The reference's own sort + sweep (src/cpu/sweep.cpp:72-157, driven as
+    app/main.cpp:147-151 drives it): canonical sorted unique pairs."""
+    boxes = np.ascontiguousarray(boxes)
+    p = _vp()
+    L = ref_lib()
+    n = L.ref_broadphase(boxes.ctypes.data, boxes.shape[0], threads, ctypes.byref(p))
+    if n == 0:
+        L.ref_free(p)
+        return np.zeros((0, 2), np.int32)
+    raw = np.ctypeslib.as_array(ctypes.cast(p, ctypes.POINTER(ctypes.c_int32)), shape=(n * 2,)).reshape(n, 2).copy()
+    L.ref_free(p)
+    return canonical(raw, threads)
