@@ -13,8 +13,10 @@ between steps); `e2e` times the same step through the C ABI on host buffers
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl stq|reference]
 
---impl reference times the reference's CPU sweep restated in oracle/ (the
-reference library itself cannot be built here) on the host cores.
+--impl reference times the reference's CPU sort + sweep on the host cores: the
+oracle restatement of src/cpu (checked bit for bit against the reference's own
+src/cpu compiled unchanged, where its source tree is present), each step a
+bounded sample of the same scene (all boxes sorted, every k-th start box swept).
 Under torchrun (N > 1) every rank runs an independent replica (the path does
 not shard on one scene); rank 0 prints the JSON line.
 """
@@ -154,23 +156,44 @@ def job_rate(units_per_rank: int, world: int, seconds_max: float) -> float:
     return world * units_per_rank / seconds_max
 
 
-def cpu_baseline(stq, orc, boxes, budget_s: float, threads: int = 0):
-    """Oracle sort of all boxes + sweep of every stride-th start box, scaled to
-    the full scene: boxes/s of the reference's CPU algorithm on this host."""
-    n = len(boxes)
-    t_sort, t_sweep, _ = orc.time_sample(boxes, 1024, threads)
-    est_full = t_sweep * 1024
+def pick_stride(orc, boxes, step_s: float, threads: int = 0) -> int:
+    """Start-box stride of a CPU sample whose sweep takes about step_s seconds
+    (a power of two, from a probe that sweeps every 256th start box)."""
+    _, t_probe, _ = orc.time_sample(boxes, 256, threads)
+    full = max(t_probe * 256, 1e-6)
     stride = 1
-    while est_full / stride > budget_s * 0.5 and stride < (1 << 20):
+    while full / stride > step_s and stride < (1 << 20):
         stride *= 2
-    if stride != 1024:
+    return stride
+
+
+def cpu_sample_steps(orc, boxes, stride: int, steps: int, warmup: int = 0, threads: int = 0) -> dict:
+    """Times the reference's CPU sort + sweep (the oracle restatement of
+    src/cpu/sweep.cpp) on a bounded sample of the scene: each step sorts all
+    boxes (from an unsorted copy) and sweeps every stride-th start box of the
+    sorted order in full. Throughput = start boxes swept / measured step time
+    (no extrapolation to the whole scene)."""
+    n = len(boxes)
+    per_step = (n + stride - 1) // stride
+    times, sorts = [], []
+    for i in range(warmup + steps):
         t_sort, t_sweep, _ = orc.time_sample(boxes, stride, threads)
-    t_full = t_sort + t_sweep * stride
+        if i >= warmup:
+            times.append(t_sort + t_sweep)
+            sorts.append(t_sort)
     th = threads if threads > 0 else orc.default_threads()
-    return dict(value=n / t_full, unit="boxes/s", cores=th, kind="port",
-                sample=(f"oracle sort of all {n} boxes ({t_sort:.2f} s) + sweep of every {stride}-th "
-                        f"start box ({t_sweep:.2f} s), scaled x{stride}"),
-                t_sort_s=t_sort, t_sweep_sample_s=t_sweep, stride=stride, t_full_s=t_full)
+    total = sum(times)
+    return dict(value=per_step * steps / total, unit="boxes/s", cores=th, kind="port",
+                sample=(f"each step: sort of all {n} boxes ({1e3 * sum(sorts) / steps:.0f} ms) + full sweep of every "
+                        f"{stride}-th start box of the sorted order ({per_step} start boxes), {th} threads; "
+                        f"boxes/s = start boxes swept / measured step time"),
+                ms_per_step=1e3 * total / steps, stride=stride, start_boxes_per_step=per_step)
+
+
+def workload_config(name: str, nV: int, nE: int, nF: int) -> dict:
+    """The `config` of both bench arms (identical by construction)."""
+    return {"workload": name, "boxes": nV + nE + nF, "vertices": nV, "edges": nE, "faces": nF,
+            "l2": "inputs and sorted scene exceed the 129 MB L2; GPU steps also flush L2 (512 MB write)"}
 
 
 def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
@@ -369,32 +392,29 @@ def bench_serving(stq, local, n_requests, rate, seed=4):
 
 
 def run_reference(args, w):
+    """The reference's CPU path on the host cores (the oracle restatement of
+    src/cpu: sort along x + sweep, app/main.cpp:138-156 scope), on the same
+    scene as the GPU arm. A CPU-only process: it loads the oracle library only
+    (which also holds the scene generators)."""
     import __graft_entry__ as entry
 
-    pkg = entry.load_package()
-    stq = pkg.stq
     orc = entry.load_oracle()
     orc.build()
-    mesh = make_mesh(stq, w)
-    boxes = orc.construct_boxes(mesh.V0, mesh.V1, mesh.E, mesh.F, stq.AABB_DTYPE)
-    n = len(boxes)
-    probe = cpu_baseline(stq, orc, boxes, budget_s=args.ref_step_s)
-    stride = probe["stride"]
-    times = []
-    for i in range(args.warmup + args.steps):
-        t_sort, t_sweep, _ = orc.time_sample(boxes, stride, 0)
-        if i >= args.warmup:
-            times.append(t_sort + t_sweep * stride)
-    t = sum(times) / len(times)
-    value = n / t
+    if w["kind"] == "crumpled":
+        V0, V1, E, F = orc.crumpled_sheets(w["sheets"], w["g"], w["amp"], w["sigma"], w["seed"])
+    else:
+        V0, V1, E, F = orc.cloth_pair(w["g"], w["z_offset"], w["sigma"], w["seed"])
+    boxes = orc.construct_boxes(V0, V1, E, F, orc.AABB_DTYPE)
+    stride = pick_stride(orc, boxes, args.ref_step_s)
+    cb = cpu_sample_steps(orc, boxes, stride, args.steps, args.warmup)
+    value = cb["value"]
     line = {
         "metric": "boxes/s (STQ broad phase, one scene)", "value": value, "unit": "boxes/s",
         "impl": "reference", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": t * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32", "data": "synthetic",
-        "config": {"workload": args.workload, "boxes": n, "host_threads": probe["cores"]},
-        "cpu_baseline": {"value": value, "unit": "boxes/s", "cores": probe["cores"], "kind": "port",
-                         "sample": probe["sample"]},
+        "ms_per_step": cb["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded crumpled-sheet trajectories)",
+        "config": workload_config(args.workload, V0.shape[0], E.shape[0], F.shape[0]),
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": value, "unit": "boxes/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -407,8 +427,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="stq", choices=["stq", "reference"])
     ap.add_argument("--workload", default="crumpled16x250", choices=sorted(WORKLOADS))
-    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
-    ap.add_argument("--ref-step-s", type=float, default=12.0)
+    ap.add_argument("--cpu-step-s", type=float, default=3.0,
+                    help="seconds of CPU sweep per sample step of the CPU baseline")
+    ap.add_argument("--cpu-steps", type=int, default=3)
+    ap.add_argument("--ref-step-s", type=float, default=3.0,
+                    help="seconds of CPU sweep per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
@@ -531,9 +554,9 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded crumpled-sheet trajectories; the reference's mesh benchmarks are not distributed)",
-        "config": {"workload": args.workload, "boxes": n, "vertices": nV, "edges": nE, "faces": nF,
-                   "pairs": npairs, "axis": "max-variance", "l2": "flushed between steps (512 MB write)",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "tuned": tuned},
+        "config": workload_config(args.workload, nV, nE, nF),
+        "pairs": npairs, "axis": "max-variance", "parallelism": "replicas" if world > 1 else "single GPU",
+        "tuned": tuned,
         "pairs_per_s": world * npairs / (ms_per_step / 1e3),
         "stage_ms_per_step": {k: v[0] / args.steps for k, v in stages.items() if v[1]},
         "gpu_launches": launches,
@@ -609,7 +632,7 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = entry.load_oracle()
         hb = orc.construct_boxes(mesh.V0, mesh.V1, mesh.E, mesh.F, stq.AABB_DTYPE)
-        cb = cpu_baseline(stq, orc, hb, budget_s=args.cpu_budget_s)
+        cb = cpu_sample_steps(orc, hb, pick_stride(orc, hb, args.cpu_step_s), args.cpu_steps, 1)
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     ctx.close()
     if dist:

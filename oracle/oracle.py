@@ -132,6 +132,41 @@ def default_threads() -> int:
     return int(lib().oracle_default_threads())
 
 
+# ---- the benchmark's synthetic inputs, from the generators linked into the
+# oracle library (the same source as the package's), for CPU-only processes --
+def _grid_counts(g: int) -> tuple[int, int, int]:
+    nv, ne, nf = _i64(), _i64(), _i64()
+    lib().stq_grid_counts(ctypes.c_int(g), ctypes.byref(nv), ctypes.byref(ne), ctypes.byref(nf))
+    return nv.value, ne.value, nf.value
+
+
+def crumpled_sheets(sheets: int, g: int, amp: float, sigma: float, seed: int):
+    """V0, V1, E, F of `sheets` crumpled g x g sheets (scenes.h stq_scene_crumpled)."""
+    nv, ne, nf = _grid_counts(g)
+    V0, V1 = np.empty((sheets * nv, 3)), np.empty((sheets * nv, 3))
+    E, F = np.empty((sheets * ne, 2), np.int32), np.empty((sheets * nf, 3), np.int32)
+    lib().stq_scene_crumpled(ctypes.c_int(sheets), ctypes.c_int(g), ctypes.c_double(amp), ctypes.c_double(sigma),
+                             ctypes.c_uint64(seed), V0.ctypes.data_as(_vp), V1.ctypes.data_as(_vp),
+                             E.ctypes.data_as(_vp), F.ctypes.data_as(_vp))
+    return V0, V1, E, F
+
+
+def cloth_pair(g: int, z_offset: float, sigma: float, seed: int, angle_deg: float = 10.0):
+    """V0, V1, E, F of a cloth pair (scenes.h stq_scene_cloth_pair)."""
+    nv, ne, nf = _grid_counts(g)
+    V0, V1 = np.empty((2 * nv, 3)), np.empty((2 * nv, 3))
+    E, F = np.empty((2 * ne, 2), np.int32), np.empty((2 * nf, 3), np.int32)
+    lib().stq_scene_cloth_pair(ctypes.c_int(g), ctypes.c_double(z_offset), ctypes.c_double(angle_deg),
+                               ctypes.c_double(sigma), ctypes.c_uint64(seed), V0.ctypes.data_as(_vp),
+                               V1.ctypes.data_as(_vp), E.ctypes.data_as(_vp), F.ctypes.data_as(_vp))
+    return V0, V1, E, F
+
+
+# the 44-byte box record (id, min, max, vertex ids, ref_id)
+AABB_DTYPE = np.dtype([("id", "<i4"), ("min", "<f4", (3,)), ("max", "<f4", (3,)),
+                       ("vertex_ids", "<i4", (3,)), ("ref_id", "<i4")])
+
+
 # ---- the reference's own CPU code (oracle/_ref), where it could be built ------
 _ref = None
 
