@@ -199,7 +199,8 @@ def workload_config(name: str, nV: int, nE: int, nF: int) -> dict:
 def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
     """256 cloth-pair scenes (box counts log-uniform in [1e3, 2e5]): the fused,
     graph-captured batch call against the per-scene plain launch loop
-    (build + prepare + sweep with its host synchronisations, scene by scene)."""
+    (build + prepare + sweep with its host synchronisations, scene by scene),
+    both with the settings the autotuner picks on this batch (untimed)."""
     meshes = stq.batch_scenes(256, 1e3, 2e5, seed=2)
     V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
     d = [torch.from_numpy(x).to(dev) for x in (V0, V1, E, F)]
@@ -211,6 +212,10 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
     total = r.total
     cap = int(total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    bboxes = torch.empty((N, 11), dtype=torch.int32, device=dev)
+    bo = ctx.batch_build_boxes(d[0], d[1], vo, d[2], eo, d[3], fo, bboxes)
+    tune_ms, tuned = ctx.autotune(bboxes, bo, pairs, cap)
+    del bboxes
 
     def timed(fn):
         for _ in range(warmup):
@@ -246,7 +251,8 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
     return {"workload": "256 cloth-pair scenes, boxes log-uniform in [1e3, 2e5]", "boxes": N,
             "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain,
             "batched_boxes_per_s": N / (t_batch / 1e3), "plain_loop_boxes_per_s": N / (t_plain / 1e3),
-            "batched_over_plain": t_plain / t_batch, "graph": True}
+            "batched_over_plain": t_plain / t_batch, "graph": True, "tuned": tuned,
+            "tuned_prepare_sweep_ms": tune_ms}
 
 
 def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush):
@@ -322,7 +328,7 @@ def bench_scene(stq, torch, dev, stream, local, steps, warmup, flush, workload):
     total = ctx.sweep_prepared(pairs, cap).total
     cap = int(total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
-    ctx.autotune(boxes, [0, n], pairs, cap)
+    _, tuned = ctx.autotune(boxes, [0, n], pairs, cap)
 
     def step():
         ctx.build_boxes(V0, V1, E, F, boxes)
@@ -343,16 +349,19 @@ def bench_scene(stq, torch, dev, stream, local, steps, warmup, flush, workload):
         ms += a.elapsed_time(b)
     ms /= steps
     ctx.close()
-    return {"workload": workload, "boxes": n, "pairs": int(total), "ms_per_step": ms,
+    return {"workload": workload, "boxes": n, "pairs": int(total), "ms_per_step": ms, "tuned": tuned,
             "boxes_per_s": n / (ms / 1e3), "pairs_per_s": total / (ms / 1e3),
             "pipeline_alg_frac": (60 * n + 8 * total) / (ms / 1e3) / 1e9 / measured_peak()[0]}
 
 
-def bench_serving(stq, local, n_requests, rate, seed=4):
+def bench_serving(stq, local, n_requests, rates, seed=4):
     """Poisson arrivals of time-stepped cloth-pair requests (boxes log-uniform
-    in [1e4, 2e6], 1-20 steps, step noise 0.003, HBM budget 160 GB): the
-    continuous-batching server against the same server run one request at a
-    time (serial). Latency = completion - arrival."""
+    in [1e4, 2e6], 1-20 steps, step noise 0.003, HBM budget 160 GB) at each
+    rate: the continuous-batching server against the same server run one
+    request at a time (serial). Latency = completion - arrival, split into the
+    wait before the request's first tick (queue and admission; its upload
+    overlaps the tick in flight) and the time from that tick's launch to
+    completion (its steps, one per tick)."""
     import numpy as np
 
     rng = np.random.default_rng(seed)
@@ -362,33 +371,53 @@ def bench_serving(stq, local, n_requests, rate, seed=4):
         m = stq.cloth_pair(g=stq.cloth_pair_grid_for(int(n)), z_offset=float(rng.uniform(0.002, 0.05)),
                            sigma=float(rng.uniform(0.001, 0.01)), seed=stq.splitmix64(seed * 7919 + k))
         reqs.append((m, int(rng.integers(1, 21)), k))
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_requests))
-    out = {}
-    for label, max_scenes in (("batched", 256), ("serial", 1)):
-        sv = stq.Server(local, None, budget_bytes=160 << 30, max_boxes=1 << 25, max_scenes=max_scenes)
-        t0 = time.perf_counter()
-        i, arrive, done = 0, {}, {}
-        while len(done) < n_requests:
-            now = time.perf_counter() - t0
-            while i < n_requests and arrivals[i] <= now:
-                m, steps, sd = reqs[i]
-                arrive[sv.submit(m, steps, 0.003, sd)] = arrivals[i]
-                i += 1
-            for rid in sv.tick():
-                done[rid] = time.perf_counter() - t0
-            st = sv.stats()
-            if st["active"] == 0 and st["queued"] == 0 and i < n_requests:
-                time.sleep(max(0.0, min(0.002, arrivals[i] - (time.perf_counter() - t0))))
-        elapsed = time.perf_counter() - t0
-        lat = np.array([done[r] - arrive[r] for r in done])
-        pairs = sum(int(sv.result(r)[0].sum()) for r in done)
-        box_steps = sum(m.num_boxes * s for m, s, _ in reqs)
-        out[label] = {"p50_ms": float(np.percentile(lat, 50) * 1e3), "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                      "pairs_per_s": pairs / elapsed, "box_steps_per_s": box_steps / elapsed,
-                      "seconds": elapsed, "ticks": sv.stats()["ticks"]}
-        sv.close()
-    return {"workload": f"{n_requests} Poisson requests at {rate} req/s; cloth pairs, boxes log-uniform "
-                        "in [1e4, 2e6], 1-20 steps, step noise 0.003; budget 160 GB", **out}
+    gaps = rng.exponential(1.0, n_requests)  # unit-rate gaps, scaled per rate
+    box_steps = sum(m.num_boxes * s for m, s, _ in reqs)
+    table = []
+    for rate in rates:
+        arrivals = np.cumsum(gaps / rate)
+        row = {"rate_per_s": rate}
+        for label, max_scenes in (("batched", 256), ("serial", 1)):
+            sv = stq.Server(local, None, budget_bytes=160 << 30, max_boxes=1 << 25, max_scenes=max_scenes)
+            t0 = time.perf_counter()
+            i, arrive, done, tick_t = 0, {}, {}, []
+            while len(done) < n_requests:
+                now = time.perf_counter() - t0
+                while i < n_requests and arrivals[i] <= now:
+                    m, steps, sd = reqs[i]
+                    arrive[sv.submit(m, steps, 0.003, sd)] = arrivals[i]
+                    i += 1
+                finished = sv.tick()
+                t_tick = time.perf_counter() - t0
+                for rid in finished:
+                    done[rid] = t_tick
+                st = sv.stats()
+                while len(tick_t) < st["ticks"]:  # the tick just launched
+                    tick_t.append(t_tick)
+                if st["active"] == 0 and st["queued"] == 0 and i < n_requests:
+                    time.sleep(max(0.0, min(0.002, arrivals[i] - (time.perf_counter() - t0))))
+            elapsed = time.perf_counter() - t0
+            lat, wait, serve, per_tick = [], [], [], []
+            for r in done:
+                first, last = sv.request_ticks(r)
+                lat.append(done[r] - arrive[r])
+                wait.append(max(0.0, tick_t[first] - arrive[r]))
+                serve.append(done[r] - tick_t[first])
+                per_tick.append((done[r] - tick_t[first]) / (last - first + 1))
+            pairs = sum(int(sv.result(r)[0].sum()) for r in done)
+            ms = lambda v, q: float(np.percentile(v, q) * 1e3)  # noqa: E731
+            row[label] = {"p50_ms": ms(lat, 50), "p99_ms": ms(lat, 99),
+                          "pairs_per_s": pairs / elapsed, "box_steps_per_s": box_steps / elapsed,
+                          "seconds": elapsed, "ticks": sv.stats()["ticks"],
+                          "wait_p50_ms": ms(wait, 50), "in_service_p50_ms": ms(serve, 50),
+                          "tick_p50_ms": ms(per_tick, 50)}
+            sv.close()
+        table.append(row)
+    return {"workload": f"{n_requests} Poisson requests per rate; cloth pairs, boxes log-uniform "
+                        "in [1e4, 2e6], 1-20 steps, step noise 0.003; budget 160 GB",
+            "latency_split": "wait = arrival to the launch of the request's first tick; in_service = "
+                             "that launch to completion; tick = in_service / its ticks (one step each)",
+            "rates": table}
 
 
 def run_reference(args, w):
@@ -441,7 +470,7 @@ def main():
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (use the library defaults), e.g. for profiling")
     ap.add_argument("--serve-requests", type=int, default=48)
-    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-rates", type=str, default="50,200,500,1000,2000")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     w = WORKLOADS[args.workload]
@@ -608,11 +637,13 @@ def main():
         h2d_ms = link_ms(lambda: [d.copy_(h, non_blocking=True) for d, h in zip((V0, V1, E, F), hmesh_t)])
         d2h_ms = link_ms(lambda: hpairs_t[:npairs].copy_(pairs[:npairs], non_blocking=True))
         e2e_s = max_over_ranks(dist, sum(ts) / len(ts), dev)
+        ts_sorted = sorted(ts)
         line["e2e"] = {"value": job_rate(n, world, e2e_s), "unit": "boxes/s",
                        "h2d_bytes_per_step": 48 * nV + 8 * nE + 12 * nF,
                        "d2h_bytes_per_step": 8 * er.count, "ms_per_step": e2e_s * 1e3,
                        "call": "stq_broadphase_host",
                        "pairs_out": "sweep windows, each copied while later ones are swept",
+                       "ms_median": 1e3 * ts_sorted[len(ts) // 2], "ms_min": 1e3 * ts_sorted[0],
                        "one_copy_after_sweep_ms_per_step": 1e3 * sum(ts_staged) / len(ts_staged),
                        "link_alone_ms": {"h2d_mesh": h2d_ms, "d2h_pairs": d2h_ms,
                                          "d2h_gbs": 8 * npairs / d2h_ms / 1e6}}
@@ -627,7 +658,8 @@ def main():
         line["skewed"] = bench_skewed(stq, torch, dev, stream, local, args.steps, args.warmup, flush)
 
     if not args.no_serve and rank == 0:
-        line["serve"] = bench_serving(stq, local, args.serve_requests, args.serve_rate)
+        line["serve"] = bench_serving(stq, local, args.serve_requests,
+                                      [float(x) for x in args.serve_rates.split(",")])
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         orc = entry.load_oracle()

@@ -75,6 +75,7 @@ void apply_options(stq_context *ctx) {
   if (ctx->options[STQ_OPT_BLOCK_SIZE]) t.block = int(ctx->options[STQ_OPT_BLOCK_SIZE]);
   if (ctx->options[STQ_OPT_CANDIDATES_PER_LANE]) t.per_lane = int(ctx->options[STQ_OPT_CANDIDATES_PER_LANE]);
   if (ctx->options[STQ_OPT_RUN_CAP]) t.run_cap = int(ctx->options[STQ_OPT_RUN_CAP]);
+  if (ctx->options[STQ_OPT_SWEEP_SHAPE]) t.shape = int(ctx->options[STQ_OPT_SWEEP_SHAPE]);
   ctx->tuning = t;
   ctx->cell_scale = ctx->options[STQ_OPT_CELL_SCALE] ? float(ctx->options[STQ_OPT_CELL_SCALE]) : 2.f;
   ctx->budget = ctx->options[STQ_OPT_REPLICA_BUDGET] ? int(ctx->options[STQ_OPT_REPLICA_BUDGET]) : 4;
@@ -247,6 +248,7 @@ int ensure_replica_buffers(stq_context *ctx, int64_t rep_cap, int64_t cells_cap)
   STQ_CUDA(ctx, ctx->sflag.ensure(sizeof(int) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->sfloor.ensure(sizeof(float2) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->partner.ensure(sizeof(int) * slots), "allocate sorted scene");
+  STQ_CUDA(ctx, ctx->run_end.ensure(sizeof(int) * slots), "allocate sorted scene");
   STQ_CUDA(ctx, ctx->cell_floor.ensure(sizeof(float2) * size_t(segs / 3 + 1)), "allocate cell bounds");
   STQ_CUDA(ctx, ctx->long_list.ensure(sizeof(int2) * slots), "allocate long-run list");
   ctx->rep_cap = int64_t(r);
@@ -316,6 +318,7 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   ctx->scene.sflag = ctx->sflag.as<int>();
   ctx->scene.sfloor = ctx->sfloor.as<float2>();
   ctx->scene.partner = ctx->partner.as<int>();
+  ctx->scene.run_end = ctx->run_end.as<int>();
   stage_begin(ctx, kGather);
   STQ_CUDA(ctx, launch_list_offsets(ctx->stream, kb[which], b.hdr, b.seg_scan, b.seg_cap, ctx->scene, ctx->slot_cap),
            "launch list offsets");
@@ -381,6 +384,7 @@ int run_sweep(stq_context *ctx, int64_t begin, int64_t end, stq_pair *pairs,
   p.sflag = ctx->scene.sflag;
   p.sfloor = ctx->scene.sfloor;
   p.partner = ctx->scene.partner;
+  p.run_end = ctx->scene.run_end;
   p.scene_pairs = ctx->scene_pairs.as<unsigned long long>();
   p.hdr = hdr;
   p.stats = &hdr->candidates;
@@ -465,7 +469,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts, &ctx->box_cells,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
-                      &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->long_list,
+                      &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->run_end, &ctx->long_list,
                       &ctx->seg_scan, &ctx->bkeys[0], &ctx->bkeys[1],
                       &ctx->bvals[0], &ctx->bvals[1],
                       &ctx->box_counts, &ctx->prefix_ws, &ctx->pair_keys[0], &ctx->pair_keys[1],
@@ -501,7 +505,7 @@ int stq_context_set_stream(stq_context *ctx, void *stream) {
 }
 
 int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
-  if (!ctx || option < 1 || option > 12 || value < 0) return STQ_ERR_INVALID_ARG;
+  if (!ctx || option < 1 || option > 13 || value < 0) return STQ_ERR_INVALID_ARG;
   auto pow2_in = [](int64_t v, int64_t lo, int64_t hi) {
     return v == 0 || (v >= lo && v <= hi && (v & (v - 1)) == 0);
   };
@@ -510,7 +514,7 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
       if (!pow2_in(value, 1, 32)) return fail(ctx, STQ_ERR_INVALID_ARG, "lanes per entry: 1..32, power of 2");
       break;
     case STQ_OPT_QUEUE_DEPTH:
-      if (!pow2_in(value, 32, 128)) return fail(ctx, STQ_ERR_INVALID_ARG, "queue depth: 32, 64 or 128");
+      if (!pow2_in(value, 16, 128)) return fail(ctx, STQ_ERR_INVALID_ARG, "queue depth: 16, 32, 64 or 128");
       break;
     case STQ_OPT_BLOCK_SIZE:
       if (!pow2_in(value, 128, 512)) return fail(ctx, STQ_ERR_INVALID_ARG, "block size: 128, 256 or 512");
@@ -544,6 +548,9 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
       if (value == 1 || value > stq_context::kCopyWindows)
         return fail(ctx, STQ_ERR_INVALID_ARG, "host windows: 2..32");
       break;
+    case STQ_OPT_SWEEP_SHAPE:
+      if (value > 2) return fail(ctx, STQ_ERR_INVALID_ARG, "sweep shape: 1 queue, 2 flat");
+      break;
     default:
       break;
   }
@@ -553,7 +560,7 @@ int stq_context_set_option(stq_context *ctx, int option, int64_t value) {
 }
 
 int64_t stq_context_get_option(const stq_context *ctx, int option) {
-  if (!ctx || option < 1 || option > 12) return -1;
+  if (!ctx || option < 1 || option > 13) return -1;
   switch (option) {
     case STQ_OPT_LANES_PER_ENTRY: return ctx->tuning.lanes;
     case STQ_OPT_QUEUE_DEPTH: return ctx->tuning.queue;
@@ -566,6 +573,7 @@ int64_t stq_context_get_option(const stq_context *ctx, int option) {
     case STQ_OPT_CANDIDATES_PER_LANE: return ctx->tuning.per_lane;
     case STQ_OPT_RUN_CAP: return ctx->tuning.run_cap;
     case STQ_OPT_HOST_WINDOWS: return ctx->options[STQ_OPT_HOST_WINDOWS] ? ctx->options[STQ_OPT_HOST_WINDOWS] : 16;
+    case STQ_OPT_SWEEP_SHAPE: return ctx->tuning.shape;
     default: return ctx->options[option];
   }
 }
@@ -1138,9 +1146,10 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   *best_ms = 0.0;
   const int64_t key = (int64_t(bits_for(std::max<int64_t>(h_box_off[n_scenes], 1))) << 32) |
                       int64_t(bits_for(n_scenes));
-  constexpr int kOpts = 6;
+  constexpr int kOpts = 7;
   const int opts[kOpts] = {STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH, STQ_OPT_BLOCK_SIZE,
-                           STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE, STQ_OPT_CANDIDATES_PER_LANE};
+                           STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE, STQ_OPT_CANDIDATES_PER_LANE,
+                           STQ_OPT_SWEEP_SHAPE};
   for (const auto &kv : ctx->tuned)
     if (kv.first == key) {
       for (int o = 0; o < kOpts; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], kv.second[size_t(o)]));
@@ -1151,9 +1160,11 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   STQ_CUDA(ctx, cudaEventCreate(&e0), "create event");
   STQ_CUDA(ctx, cudaEventCreate(&e1), "create event");
+  // each setting: the fastest of kReps timed runs (the GPU may be shared)
+  constexpr int kReps = 5;
   auto elapsed = [&](const std::function<int()> &fn, float *ms) -> int {
     float best = 1e30f;
-    for (int rep = 0; rep < 2; ++rep) {
+    for (int rep = 0; rep < kReps; ++rep) {
       STQ_CUDA(ctx, cudaEventRecord(e0, ctx->stream), "record");
       STQ_TRY(fn());
       STQ_CUDA(ctx, cudaEventRecord(e1, ctx->stream), "record");
@@ -1165,41 +1176,57 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
     *ms = best;
     return STQ_OK;
   };
+  // a sweep setting: shape, lanes per entry, candidates per lane (or filter
+  // steps of the flat shape), queue depth, block size
+  struct Shape {
+    int64_t shape, lanes, per_lane, queue, block;
+  };
+  std::vector<Shape> space;
+  for (int64_t per_lane : {2, 4, 8})  // one start box per lane: the ring holds >= 32
+    for (int64_t queue : {32, 64})
+      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, 1, per_lane, queue, block});
+  for (int64_t lanes : {4, 8, 16})  // lane groups sharing a start box
+    for (int64_t queue : {16, 32, 64})
+      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, lanes, 8, queue, block});
+  for (int64_t steps : {2, 4})  // flat: runs of 32 start boxes end to end
+    for (int64_t block : {128, 256}) space.push_back({kShapeFlat, 1, steps, 64, block});
   std::vector<int64_t> best_set(kOpts, 0);
-  // sweep shapes: one start box per lane with 2, 4 or 8 candidates per step,
-  // or lane groups of 4, 8 or 16 lanes sharing one start box
-  const int64_t shapes[6][2] = {{1, 2}, {1, 4}, {1, 8}, {4, 0}, {8, 0}, {16, 0}};
   float best_total = 1e30f;
   int st = STQ_OK;
   for (int64_t scale : {1, 2, 4}) {
+    if ((st = stq_context_set_option(ctx, STQ_OPT_CELL_SCALE, scale)) != STQ_OK) break;
+    // the radix width changes the prepare only: the sorted scene is the same
+    float t_prep = 1e30f;
+    int64_t best_radix = 8;
     for (int64_t radix : {8, 4}) {
-      if ((st = stq_context_set_option(ctx, STQ_OPT_CELL_SCALE, scale)) != STQ_OK) break;
       if ((st = stq_context_set_option(ctx, STQ_OPT_RADIX_BITS, radix)) != STQ_OK) break;
-      float t_prep = 0.f;
+      float t = 0.f;
       st = elapsed([&] { return stq_batch_prepare(ctx, d_boxes, h_box_off, n_scenes, nullptr, STQ_AXIS_AUTO); },
-                   &t_prep);
+                   &t);
       if (st != STQ_OK) break;
-      for (const auto &shape : shapes)
-        for (int64_t queue : {32, 64, 128})
-          for (int64_t block : {128, 256, 512}) {
-            const int64_t lanes = shape[0], per_lane = shape[1];
-            stq_context_set_option(ctx, STQ_OPT_LANES_PER_ENTRY, lanes);
-            stq_context_set_option(ctx, STQ_OPT_CANDIDATES_PER_LANE, per_lane);
-            stq_context_set_option(ctx, STQ_OPT_QUEUE_DEPTH, queue);
-            stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, block);
-            float t_sweep = 0.f;
-            int64_t count = 0, next = 0, total = 0;
-            st = elapsed([&] {
-              const int r = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, &count, &next, &total);
-              return r == STQ_OVERFLOW ? STQ_OK : r;
-            }, &t_sweep);
-            if (st != STQ_OK) break;
-            if (t_prep + t_sweep < best_total) {
-              best_total = t_prep + t_sweep;
-              best_set = {lanes, queue, block, radix, scale, per_lane};
-            }
-          }
+      if (t < t_prep) {
+        t_prep = t;
+        best_radix = radix;
+      }
+    }
+    if (st != STQ_OK) break;
+    for (const Shape &sh : space) {
+      stq_context_set_option(ctx, STQ_OPT_SWEEP_SHAPE, sh.shape);
+      stq_context_set_option(ctx, STQ_OPT_LANES_PER_ENTRY, sh.lanes);
+      stq_context_set_option(ctx, STQ_OPT_CANDIDATES_PER_LANE, sh.per_lane);
+      stq_context_set_option(ctx, STQ_OPT_QUEUE_DEPTH, sh.queue);
+      stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, sh.block);
+      float t_sweep = 0.f;
+      int64_t count = 0, next = 0, total = 0;
+      st = elapsed([&] {
+        const int r = stq_sweep_prepared(ctx, 0, 0, d_pairs, capacity, &count, &next, &total);
+        return r == STQ_OVERFLOW ? STQ_OK : r;
+      }, &t_sweep);
       if (st != STQ_OK) break;
+      if (t_prep + t_sweep < best_total) {
+        best_total = t_prep + t_sweep;
+        best_set = {sh.lanes, sh.queue, sh.block, best_radix, scale, sh.per_lane, sh.shape};
+      }
     }
     if (st != STQ_OK) break;
   }

@@ -513,6 +513,7 @@ list_offsets_kernel(const unsigned long long *__restrict__ keys, BatchHeader *__
       scene.xmin[k] = q;
       scene.xmax[k] = q;
       scene.partner[k] = int(k);
+      scene.run_end[k] = int(k);
     }
   };
   uint32_t mx = 0;
@@ -592,7 +593,7 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
                     float *__restrict__ xmax,
                     const float2 *__restrict__ cell_floor, float4 *__restrict__ syz,
                     int4 *__restrict__ sv, int *__restrict__ sflag, float2 *__restrict__ sfloor,
-                    int *__restrict__ partner) {
+                    int *__restrict__ partner, int *__restrict__ run_end) {
   const int64_t R = hdr->replicas;
   const int S = hdr->n_scenes;
   for (int64_t p = blockIdx.x * int64_t(kBlock) + threadIdx.x; p < R;
@@ -617,11 +618,16 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
     const int fc = cell_coord(x.min[c], g.oc, g.ic, g.nc) == cc;
     const int64_t k = p + seg;
     int64_t first = k + 1;
+    // the candidate list: the edge's own list after it, or the other type's
+    // list of the cell from the bound search below
+    unsigned int cand = seg;
+    uint32_t run_a = uint32_t(p) + 1u, run_e = seg_scan[seg + 1];
     if (type != 1u) {
       // bound search of this min among the other list's sorted keys
       const unsigned int other = 3u * cell + (type == 0u ? 2u : 0u);
       const uint32_t xk = uint32_t(key & 0xffffffffu);
       uint32_t a = seg_scan[other], e = seg_scan[other + 1];
+      run_e = e;
       while (a < e) {
         const uint32_t mid = (a + e) >> 1;
         const uint32_t mk = uint32_t(keys[mid] & 0xffffffffu);
@@ -629,6 +635,26 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
         else e = mid;
       }
       first = int64_t(a) + other;
+      cand = other;
+      run_a = a;
+    }
+    if (run_end) {
+      // end of the run: the first candidate whose min is above this max
+      // (keys order as floats, -0 = +0, so the key test is the sweep's x
+      // test); galloping from the run's start, then a bisection
+      const uint32_t xk = float_key(x.max[g.axis]);
+      uint32_t a = run_a, step = 8;
+      while (a + step <= run_e && uint32_t(keys[a + step - 1] & 0xffffffffu) <= xk) {
+        a += step;
+        step <<= 1;
+      }
+      uint32_t e = min(a + step, run_e);
+      while (a < e) {
+        const uint32_t mid = (a + e) >> 1;
+        if (uint32_t(keys[mid] & 0xffffffffu) <= xk) a = mid + 1;
+        else e = mid;
+      }
+      run_end[k] = int(int64_t(a) + cand);
     }
     xmin[k] = x.min[g.axis];
     xmax[k] = x.max[g.axis];
@@ -740,7 +766,8 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
   gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
                                                              scenes, seg_scan, scene.xmin, scene.xmax,
                                                              cell_floor, scene.syz, scene.sv,
-                                                             scene.sflag, scene.sfloor, scene.partner);
+                                                             scene.sflag, scene.sfloor, scene.partner,
+                                                             scene.run_end);
   return cudaGetLastError();
 }
 

@@ -74,7 +74,7 @@ struct stq_context {
   char *in_host = nullptr;
   size_t in_host_bytes = 0;
   DevBuf scenes, cell_base, scene_pairs, counts, offsets, box_cells, scan_ws, keys64[2], vals[2], sort_ws;
-  DevBuf xmin, xmax, syz, sv, sflag, sfloor, partner, box_counts, prefix_ws, pair_keys[2];
+  DevBuf xmin, xmax, syz, sv, sflag, sfloor, partner, run_end, box_counts, prefix_ws, pair_keys[2];
   DevBuf cell_floor;  // lower bounds of each cell on b and c
   DevBuf long_list;  // runs handed from the lane sweep to the warp pass
   DevBuf seg_scan;  // first sorted replica of each (cell, type) list

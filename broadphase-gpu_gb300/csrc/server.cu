@@ -135,6 +135,7 @@ struct Request {
   void *dmem = nullptr;  // V0 | V1 | E | F on the device
   size_t oV1 = 0, oE = 0, oF = 0, bytes = 0;
   int step = 0;          // next timestep to run
+  int64_t first_tick = -1, last_tick = -1;  // ticks that ran its first and last step
   int64_t est_pairs = 0;
   int64_t footprint = 0;
   std::vector<int64_t> counts;
@@ -317,6 +318,7 @@ int collect(stq_server *sv, int64_t *done_ids, int max_done, int *n_done) {
     sv->density = 0.9 * sv->density + 0.1 * double(c) / double(std::max<int64_t>(r->boxes(), 1));
     r->step += 1;
     if (r->step >= r->steps) {
+      r->last_tick = sv->ticks - 1;
       release(r);
       sv->held -= r->footprint;
       sv->active.erase(std::find(sv->active.begin(), sv->active.end(), r));
@@ -382,7 +384,7 @@ int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t ma
   sv->fixed = int64_t(ctx->in_dev.bytes + ctx->counts.bytes + ctx->offsets.bytes + ctx->scan_ws.bytes +
                       ctx->keys64[0].bytes * 2 + ctx->vals[0].bytes * 2 + ctx->sort_ws.bytes + ctx->xmin.bytes + ctx->xmax.bytes +
                       ctx->syz.bytes + ctx->sv.bytes + ctx->sflag.bytes + ctx->sfloor.bytes +
-                      ctx->cell_floor.bytes + ctx->partner.bytes +
+                      ctx->cell_floor.bytes + ctx->partner.bytes + ctx->run_end.bytes +
                       ctx->seg_scan.bytes + ctx->batch_boxes.bytes);
   if (sv->fixed >= budget_bytes) return bad(STQ_ERR_NO_MEMORY);
   *out = sv.release();
@@ -478,6 +480,8 @@ int stq_server_tick(stq_server *sv, int64_t *done_ids, int max_done, int *n_done
   // 3. next tick over the current timestep of every active request
   if (sv->active.empty()) return STQ_OK;
   sv->batch = sv->active;
+  for (Request *r : sv->batch)
+    if (r->first_tick < 0) r->first_tick = sv->ticks;
   STQ_TRY(launch_tick(sv));
   sv->in_flight = true;
   sv->ticks += 1;
@@ -495,6 +499,16 @@ int stq_server_result(stq_server *sv, int64_t request_id, int64_t *counts, uint6
     if (counts) counts[k] = r.counts[size_t(k)];
     if (checksums) checksums[k] = r.checks[size_t(k)];
   }
+  return STQ_OK;
+}
+
+int stq_server_request_ticks(stq_server *sv, int64_t request_id, int64_t *first_tick,
+                             int64_t *last_tick) {
+  if (!sv || !first_tick || !last_tick) return STQ_ERR_INVALID_ARG;
+  auto it = sv->all.find(request_id);
+  if (it == sv->all.end()) return STQ_ERR_INVALID_ARG;
+  *first_tick = it->second->first_tick;
+  *last_tick = it->second->last_tick;
   return STQ_OK;
 }
 

@@ -151,6 +151,7 @@ extern "C" int stq_sweep_static(const stq_aabb *d_boxes, int64_t n, int axis, st
   p.sflag = reinterpret_cast<const int *>(scratch + kOffFlag);
   p.sfloor = reinterpret_cast<const float2 *>(scratch + kOffFloor);
   p.partner = reinterpret_cast<const int *>(scratch + kOffPartner);
+  p.run_end = nullptr;  // run ends are not computed here; the sweep takes the queue shape
   p.begin = 0;
   p.end = ni;
   p.chunk = 32;

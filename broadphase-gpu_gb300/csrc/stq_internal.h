@@ -132,8 +132,15 @@ struct TileRec {
   int scene;        // scene of the tile
 };
 
+// Sweep shapes (STQ_OPT_SWEEP_SHAPE): a per-warp ring of pending start boxes
+// taken by lanes or lane groups, or the flat shape (each warp's 32 starts'
+// runs laid end to end, one candidate per lane and step).
+constexpr int kShapeRing = 1;
+constexpr int kShapeFlat = 2;
+
 // Sweep-kernel tuning (autotuned or set through stq_context_set_option).
 struct SweepTuning {
+  int shape = kShapeRing;  // kShapeRing or kShapeFlat
   int lanes = 1;        // lanes sharing one pending start box (1..32)
   int per_lane = 8;     // lanes = 1: candidates a lane tests per step (1, 2, 4, 8)
   int run_cap = 512;    // candidates per start box before the warp pass takes over
@@ -153,6 +160,7 @@ struct SortedScene {
   float2 *sfloor = nullptr;  // per axis b, c: -inf where the cell is the box's
                              // first, else the cell's lower bound
   int *partner = nullptr; // first candidate position of each start position
+  int *run_end = nullptr; // one past its last candidate on the sweep axis
   int64_t length = 0;     // sweep positions (boxes; sentinels excluded at the end)
 };
 
@@ -191,6 +199,8 @@ struct SweepParams {
   const float2 *sfloor;      // first-cell rule of a start position on b and c:
                              // a candidate passes if its minima are >= these
   const int *partner;        // first candidate position of each start position
+  const int *run_end;        // one past its last candidate (null: not computed;
+                             // the flat shape needs it)
   unsigned long long *scene_pairs;  // per-scene pair counters
   const BatchHeader *hdr;    // device sizes (length bounds the sweep range)
   unsigned long long *stats; // candidates tested (may be null)

@@ -44,7 +44,8 @@ template <int G, int Q, int BLOCK, bool COUNT>
 __global__ void __launch_bounds__(BLOCK)
 stq_sweep_kernel(const SweepParams p) {
   static_assert(32 % G == 0, "lane group must divide the warp");
-  static_assert((Q & (Q - 1)) == 0 && Q >= 32, "queue depth: power of two >= 32");
+  // the refill tops the ring up to one entry per group: Q >= 32 / G
+  static_assert((Q & (Q - 1)) == 0 && Q >= 16 && Q >= 32 / G, "queue depth: power of two >= 16 and >= groups");
   constexpr int E = 32 / G;  // lane groups per warp
   constexpr int STAGE = 64;  // pairs staged per warp before one global append
   __shared__ int ring[BLOCK / 32][Q];
@@ -406,6 +407,194 @@ stq_sweep_lane_kernel(const SweepParams p) {
   }
 }
 
+// Flat shape. A warp takes 32 consecutive start positions; each one's run on
+// the sweep axis is [partner, run_end), both found by the gather (runs longer
+// than run_cap are cut there and the rest goes to the warp pass). The runs of
+// the starts that have candidates are laid end to end, and the warp walks
+// that flat sequence 32 candidates per step, one per lane: lane l of the step
+// at `base` takes flat candidate f = base + l, whose start is the last one
+// whose run begins at or before f (a bit mask of the run beginnings inside the
+// step, one OR-reduction, and a population count). Consecutive lanes read
+// consecutive positions of a run, and every lane works except in the last
+// step of the 32 starts.
+// Two passes per warp. The filter tests the y/z overlap and the first-cell
+// rule on the candidate's (min_b, min_c, max_b, max_c) record, V steps with
+// their loads issued together, and compacts the candidates that pass into a
+// per-warp shared-memory queue. Once 32 are queued, the check takes them one
+// per lane: the vertex ids of both boxes, is_valid_pair and covertex, and the
+// hits go through the staging buffer as in the other shapes. The starts'
+// records sit in shared memory, so the queue is drained before the next 32
+// starts replace them.
+struct FlatStart {
+  float4 kb;   // start box (min_b, min_c, max_b, max_c)
+  float2 kfl;  // first-cell rule
+  int joff;    // position of flat candidate f is joff + f
+  int kf;      // first-cell bits and scene
+  int4 kv;     // vertex ids and id
+};
+static_assert(sizeof(FlatStart) == 48, "FlatStart: three 16-byte words");
+
+template <int BLOCK, int V>
+__global__ void __launch_bounds__(BLOCK)
+stq_sweep_flat_kernel(const SweepParams p) {
+  constexpr int STAGE = 64;  // < 32 left over + at most 32 new pairs per check
+  constexpr int QUEUE = 32 * (V + 1);  // < 32 left over + at most 32 * V per filter round
+  __shared__ FlatStart recs[BLOCK / 32][32];
+  __shared__ int2 stage[BLOCK / 32][STAGE];
+  __shared__ int2 queue[BLOCK / 32][QUEUE];  // (start record, candidate position)
+
+  const int lane = threadIdx.x & 31;
+  const unsigned below = lanemask_lt();
+  const unsigned upto = below | (1u << lane);
+  FlatStart *rec = recs[threadIdx.x >> 5];
+  int2 *st = stage[threadIdx.x >> 5];
+  int2 *qu = queue[threadIdx.x >> 5];
+
+  const int end = min(p.end, int(p.hdr->length));
+  const int span = end - p.begin;
+  const bool multi = p.hdr->n_scenes > 1;
+  int next_k = 0, chunk_end = 0;
+  unsigned long long tested = 0;  // warp-uniform
+  int staged = 0, queued = 0;
+  int wscene = 0;
+  unsigned long long wpairs = 0;
+
+  // the check of n <= 32 queued candidates (the last n entries)
+  auto check = [&](int n) {
+    bool hit = false;
+    int2 pr = make_int2(0, 0);
+    int kf = 0;
+    if (lane < n) {
+      const int2 e = qu[queued - n + lane];
+      const int4 bv = p.sv[e.y];
+      const int4 kv = rec[e.x].kv;
+      if (multi) kf = rec[e.x].kf;
+      hit = (p.typed || valid_pair(kv, bv)) && !covertex(kv, bv);
+      pr = make_int2(min(kv.w, bv.w), max(kv.w, bv.w));
+    }
+    queued -= n;
+    const unsigned hm = __ballot_sync(kFullMask, hit);
+    if (hm) {
+      if (hit) st[staged + __popc(hm & below)] = pr;
+      staged += __popc(hm);
+      if (!multi) {
+        wpairs += __popc(hm);
+      } else {
+        const int lead = __shfl_sync(kFullMask, kf >> 2, __ffs(hm) - 1);
+        if (__all_sync(kFullMask, !hit || (kf >> 2) == lead)) {
+          if (lead != wscene) {
+            if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+            wscene = lead;
+            wpairs = 0;
+          }
+          wpairs += __popc(hm);
+        } else if (hit) {
+          atomicAdd(&p.scene_pairs[kf >> 2], 1ull);
+        }
+      }
+      if (staged >= 32) {
+        __syncwarp();
+        flush_staged(st, staged, lane, p);
+        staged = 0;
+      }
+    }
+  };
+
+  while (true) {
+    if (next_k >= chunk_end) {
+      int c = 0;
+      if (lane == 0) c = atomicAdd(p.work, p.chunk);
+      c = __shfl_sync(kFullMask, c, 0);
+      if (c >= span) break;
+      next_k = p.begin + c;
+      chunk_end = min(next_k + p.chunk, end);
+    }
+    const int take = min(32, chunk_end - next_k);
+    const int k = next_k + lane;
+    next_k += take;
+    // 1. Runs: the candidates before the first minimum above the start's
+    //    maximum (a sentinel position has an empty run).
+    int len = 0, j = 0;
+    if (lane < take) {
+      j = p.partner[k];
+      len = max(p.run_end[k] - j, 0);
+      if (p.run_cap && len > p.run_cap) {  // a long run: the warp pass takes the rest
+        p.long_list[atomicAdd(p.long_items, 1u)] = make_int2(k, j + p.run_cap);
+        len = p.run_cap;
+      }
+    }
+    const unsigned nz = __ballot_sync(kFullMask, len > 0);
+    if (nz == 0) continue;
+    // 2. Lay the runs end to end: exclusive prefix of the lengths; the starts
+    //    with candidates keep their records in shared memory, in lane order.
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(kFullMask, incl, o);
+      if (lane >= o) incl += v;
+    }
+    const int excl = incl - len;
+    const int total = __shfl_sync(kFullMask, incl, 31);
+    if (len > 0) {
+      FlatStart r;
+      r.kb = p.syz[k];
+      r.kfl = p.sfloor[k];
+      r.joff = j - excl;
+      r.kf = multi ? p.sflag[k] : 0;
+      r.kv = p.sv[k];
+      rec[__popc(nz & below)] = r;
+    }
+    __syncwarp();
+    tested += unsigned(total);
+    // a run that begins inside the step at `base` marks bit (excl - base)
+    const unsigned my_begin = len > 0 ? unsigned(excl) : 0xffffffffu;
+    // 3. The filter over the flat candidates, V steps of 32 at a time.
+    int begun = 0;  // starts whose run began before the current step
+    for (int base = 0; base < total; base += 32 * V) {
+      int si[V], jj[V];
+      float4 kfj[V];  // (rule b, rule c, joff, -) of each lane's start
+      float4 b[V];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        const unsigned d = my_begin - unsigned(base + 32 * v);
+        const unsigned heads = __reduce_or_sync(kFullMask, d < 32u ? (1u << d) : 0u);
+        si[v] = begun + __popc(heads & upto) - 1;
+        begun += __popc(heads);
+        const int f = base + 32 * v + lane;
+        kfj[v] = *reinterpret_cast<const float4 *>(&rec[si[v]].kfl);
+        jj[v] = f < total ? __float_as_int(kfj[v].z) + f : -1;
+      }
+#pragma unroll
+      for (int v = 0; v < V; ++v)
+        if (jj[v] >= 0) b[v] = p.syz[jj[v]];
+#pragma unroll
+      for (int v = 0; v < V; ++v) {
+        bool pass = false;
+        if (jj[v] >= 0) {
+          const float4 kb = rec[si[v]].kb;
+          // the first-cell rule as in the other shapes
+          pass = overlap_bc(kb, b[v]) && b[v].x >= kfj[v].x && b[v].y >= kfj[v].y;
+        }
+        const unsigned pm = __ballot_sync(kFullMask, pass);
+        if (pass) qu[queued + __popc(pm & below)] = make_int2(si[v], jj[v]);
+        queued += __popc(pm);
+      }
+      __syncwarp();
+      // 4. The check, 32 queued candidates at a time.
+      while (queued >= 32) {
+        check(32);
+        __syncwarp();
+      }
+    }
+    if (queued) check(queued);
+    __syncwarp();  // the records are rewritten by the next 32 starts
+  }
+  __syncwarp();
+  if (staged) flush_staged(st, staged, lane, p);
+  if (lane == 0 && wpairs) atomicAdd(&p.scene_pairs[wscene], wpairs);
+  if (lane == 0 && p.stats) atomicAdd(p.stats, tested);
+}
+
 // The warp pass over the runs the lane sweep handed over (runs longer than
 // SweepParams::run_cap, which would keep one lane or group busy long after the
 // others finished). One warp per run; each step tests 32 * U consecutive
@@ -550,6 +739,9 @@ cudaError_t launch_gq(cudaStream_t s, const SweepParams &p, int block, int sms) 
 template <int G>
 cudaError_t launch_g(cudaStream_t s, const SweepParams &p, const SweepTuning &t, int sms) {
   switch (t.queue) {
+    case 16:  // at least one entry per lane group
+      if constexpr (G >= 2) return launch_gq<G, 16>(s, p, t.block, sms);
+      else return launch_gq<G, 32>(s, p, t.block, sms);
     case 32: return launch_gq<G, 32>(s, p, t.block, sms);
     case 128: return launch_gq<G, 128>(s, p, t.block, sms);
     default: return launch_gq<G, 64>(s, p, t.block, sms);
@@ -568,10 +760,19 @@ cudaError_t launch_uq(cudaStream_t s, const SweepParams &p, int block, int sms) 
 template <int U>
 cudaError_t launch_u(cudaStream_t s, const SweepParams &p, const SweepTuning &t, int sms) {
   switch (t.queue) {
+    case 16:  // one start box per lane refills to 32 entries: the ring holds at least 32
     case 32: return launch_uq<U, 32>(s, p, t.block, sms);
     case 128: return launch_uq<U, 128>(s, p, t.block, sms);
     default: return launch_uq<U, 64>(s, p, t.block, sms);
   }
+}
+
+// The flat shape's blocks are 128 or 256 threads (512 would pass the 48 KB of
+// static shared memory a block may hold).
+template <int V>
+cudaError_t launch_flat(cudaStream_t s, const SweepParams &p, int block, int sms) {
+  if (block == 128) return launch_persistent(stq_sweep_flat_kernel<128, V>, 128, s, p, sms);
+  return launch_persistent(stq_sweep_flat_kernel<256, V>, 256, s, p, sms);
 }
 
 // ---- overflow: longest prefix of start boxes whose pairs fit ------------------
@@ -704,6 +905,12 @@ static cudaError_t launch_sweep_lanes(cudaStream_t s, const SweepParams &p, cons
                                       bool count_mode, int num_sms) {
   if (count_mode)  // per-start-box counts do not depend on the tuning
     return launch_variant<8, 64, 256, true>(s, p, num_sms);
+  if (t.shape == kShapeFlat && p.run_end) {
+    switch (t.per_lane) {  // filter steps per round
+      case 2: return launch_flat<2>(s, p, t.block, num_sms);
+      default: return launch_flat<4>(s, p, t.block, num_sms);
+    }
+  }
   if (t.lanes == 1) {  // one start box per lane
     switch (t.per_lane) {
       case 1: return launch_u<1>(s, p, t, num_sms);

@@ -43,7 +43,8 @@ STQ_ERR_NOT_PREPARED = -7
 AXIS_AUTO, AXIS_X, AXIS_Y, AXIS_Z = -1, 0, 1, 2
 OPT_LANES, OPT_QUEUE, OPT_BLOCK, OPT_CELLS, OPT_RADIX_BITS, OPT_CELL_SCALE = 1, 2, 3, 4, 5, 6
 OPT_REPLICA_BUDGET, OPT_GRAPH, OPT_HOST_OVERLAP, OPT_PER_LANE, OPT_RUN_CAP = 7, 8, 9, 10, 11
-OPT_HOST_WINDOWS = 12
+OPT_HOST_WINDOWS, OPT_SWEEP_SHAPE = 12, 13
+SHAPE_QUEUE, SHAPE_FLAT = 1, 2
 
 _c_i64p = ctypes.POINTER(ctypes.c_int64)
 _vp = ctypes.c_void_p
@@ -98,6 +99,7 @@ ABI_SIGNATURES = {
     "stq_server_result": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_int)]),
     "stq_server_mesh": (ctypes.c_int, [_vp, ctypes.c_int64, _vp, _vp]),
+    "stq_server_request_ticks": (ctypes.c_int, [_vp, ctypes.c_int64, _c_i64p, _c_i64p]),
     "stq_server_stats": (ctypes.c_int, [_vp, _c_i64p, _c_i64p, _c_i64p, _c_i64p]),
     "stq_server_set_option": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int64]),
     "stq_read_mesh": (ctypes.c_int, [ctypes.c_char_p, _vp, _c_i64p, _vp, _c_i64p]),
@@ -320,7 +322,7 @@ class Context:
         self._check(self.lib.stq_autotune(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1, _ptr(pairs),
                                           capacity, ctypes.byref(ms)))
         names = {OPT_LANES: "lanes", OPT_QUEUE: "queue", OPT_BLOCK: "block", OPT_RADIX_BITS: "radix_bits",
-                 OPT_CELL_SCALE: "cell_scale", OPT_PER_LANE: "per_lane"}
+                 OPT_CELL_SCALE: "cell_scale", OPT_PER_LANE: "per_lane", OPT_SWEEP_SHAPE: "shape"}
         return ms.value, {v: self.get_option(k) for k, v in names.items()}
 
     def batch_scene_pairs(self, n_scenes: int) -> np.ndarray:
@@ -413,6 +415,15 @@ class Server:
         if st != STQ_OK:
             raise STQError(st, "unknown request")
         return counts[: done.value].copy(), checks[: done.value].copy()
+
+    def request_ticks(self, rid: int) -> tuple:
+        """(first, last): indices of the ticks that ran the request's first and
+        last timestep (-1 until then)."""
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        st = self.lib.stq_server_request_ticks(self._h, rid, ctypes.byref(a), ctypes.byref(b))
+        if st != STQ_OK:
+            raise STQError(st, "unknown request")
+        return a.value, b.value
 
     def mesh(self, rid: int):
         nv = self._meshes[rid]

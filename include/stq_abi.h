@@ -84,7 +84,9 @@ enum { STQ_AXIS_AUTO = -1, STQ_AXIS_X = 0, STQ_AXIS_Y = 1, STQ_AXIS_Z = 2 };
 typedef enum stq_option {
   STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1 (default),
                                   2, 4, 8, 16, 32                                   */
-  STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 32, 64 (default) or 128 */
+  STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 16, 32, 64 (default) or
+                                  128; with one lane per entry the queue holds at
+                                  least 32 (16 acts as 32)                         */
   STQ_OPT_BLOCK_SIZE = 3,      /* sweep block size: 128, 256 (default) or 512     */
   STQ_OPT_CELLS = 4,           /* cell grid on the two non-sweep axes: 0 automatic,
                                   1 no cells (plain sweep), k > 1 a k x k grid      */
@@ -100,13 +102,22 @@ typedef enum stq_option {
                                   while the next is swept (default), 2 one copy
                                   after the whole sweep                            */
   STQ_OPT_CANDIDATES_PER_LANE = 10, /* with one lane per entry: candidates a lane
-                                  tests per step, 1, 2, 4 or 8 (default)        */
+                                  tests per step, 1, 2, 4 or 8 (default); with the
+                                  flat shape: steps of 32 candidates whose loads
+                                  are issued together, 2 or 4 (default 8 acts as 4) */
   STQ_OPT_RUN_CAP = 11,        /* candidates of one start box a lane (group) tests
                                   before a whole warp takes over the rest of its
                                   run (1..2^20, default 512)                      */
-  STQ_OPT_HOST_WINDOWS = 12    /* stq_sweep_host / stq_broadphase_host: windows a
+  STQ_OPT_HOST_WINDOWS = 12,   /* stq_sweep_host / stq_broadphase_host: windows a
                                   sweep is cut into (2..32, default 16; fewer when
                                   the scene has under 2^19 positions per window) */
+  STQ_OPT_SWEEP_SHAPE = 13     /* 1 (default): a per-warp queue of pending start
+                                  boxes taken by lanes or lane groups
+                                  (STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH);
+                                  2: flat, each warp lays the runs of 32 start
+                                  boxes end to end and tests one candidate per
+                                  lane and step (block size 128 or 256; 512 acts
+                                  as 256)                                          */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -258,10 +269,15 @@ int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count);
 
 /* ---- autotuning --------------------------------------------------------------
  * Times prepare + sweep of the given batch (as stq_batch_prepare, all start
- * boxes) over cell scale {1, 2, 4}, radix digit width {4, 8}, lanes per queue
- * entry {4, 8, 16, 32} (the work-split width of a start box's run), queue
- * depth {32, 64, 128} and block size {128, 256, 512}, and keeps the fastest
- * settings as the context's options. Settings are cached per shape bucket
+ * boxes), each setting five times (the fastest counts), over cell scale
+ * {1, 2, 4} and radix digit width {4, 8} (the prepare), and over the sweep
+ * shapes (the work split of the start boxes' runs): one start box per lane
+ * with 2, 4 or 8 candidates per step (queue depth {32, 64}), lane groups of
+ * 4, 8 or 16 lanes (queue depth {16, 32, 64}), each with block size
+ * {128, 256, 512}, and the flat shape with 2 or 4 filter steps per round and
+ * block size {128, 256}. Keeps the fastest prepare + sweep as the context's
+ * options (cell scale, radix width, sweep shape, lanes per entry, candidates
+ * per lane, queue depth, block size). Settings are cached per shape bucket
  * (log2 of the box count, log2 of the scene count): a later call whose batch
  * falls in a tuned bucket applies them without timing. *best_ms receives the
  * prepare + sweep time of the chosen settings (0 on a cache hit). The batch is
@@ -296,6 +312,10 @@ int stq_server_tick(stq_server *server, int64_t *done_ids, int max_done, int *n_
  * of splitmix64((lo << 32) | hi) with ids local to the request's mesh. */
 int stq_server_result(stq_server *server, int64_t request_id, int64_t *counts,
                       uint64_t *checksums, int max_steps, int *steps_done);
+/* Ticks of a request: the index (0-based, in launch order) of the tick that
+ * ran its first timestep and of the one that ran its last; -1 until then. */
+int stq_server_request_ticks(stq_server *server, int64_t request_id, int64_t *first_tick,
+                             int64_t *last_tick);
 /* Current positions of an active request (t0 and t1 of its last step). */
 int stq_server_mesh(stq_server *server, int64_t request_id, double *h_V0, double *h_V1);
 /* active, queued, bytes held for admitted requests, ticks launched */

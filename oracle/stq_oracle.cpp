@@ -5,11 +5,14 @@
 // by the tests, the smoke check and the bench's CPU baseline and reference
 // legs, to check and time against. Nothing in the product links or calls it.
 //
-// Parity status: parity unpinned by reference golden vectors. The reference
-// ships no tests, no golden vectors and no fixtures, and its CPU library
-// cannot be built here (it needs Eigen, oneTBB, spdlog and nlohmann_json
-// fetched by CMake). The restatement follows the reference source line by
-// line (citations below) and is pinned by hand-derived known-answer cases.
+// Parity status: pinned to the reference's own code. The reference ships no
+// tests, golden vectors or fixtures, but its src/cpu/aabb.cpp and
+// src/cpu/sweep.cpp compile unchanged against the stand-in headers of
+// oracle/ref_shim/ (the Eigen, oneTBB and spdlog subsets they use) into
+// oracle/_ref/libstq_ref.so. The tests check this restatement against that
+// library where the reference's tree is present, and everywhere against the
+// golden vectors it wrote (tests/golden/ref_vectors.npz). The hand-derived
+// known-answer cases of tests/golden/kat.json pin the corner cases on top.
 //
 // Build: without -ffast-math and without flush-to-zero, so that the outward
 // rounding below (which subtracts the smallest denormal) behaves as IEEE 754

@@ -60,13 +60,17 @@ def test_batch_build_matches_single_builds(ctx, stq, oracle, cuda, scenes):
         assert part.tobytes() == want.tobytes(), k
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("mixed_axes", [False, True])
 @pytest.mark.parametrize("run_cap", [0, 3])
-def test_batch_prepare_and_sweep(ctx, stq, oracle, cuda, scenes, mixed_axes, run_cap):
+def test_batch_prepare_and_sweep(ctx, stq, oracle, cuda, scenes, mixed_axes, run_cap, shape):
+    """Scene by scene against the oracle, with the per-scene pair counts
+    (queue and flat shapes)."""
     import torch
 
     meshes, want = scenes
     ctx.set_option(stq.OPT_RUN_CAP, run_cap)
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
     n = sum(m.num_boxes for m in meshes)
     boxes = torch.empty((n, 11), dtype=torch.int32, device=cuda)
@@ -103,11 +107,13 @@ def test_batch_overflow_resume(ctx, stq, oracle, cuda, scenes):
 
 
 @pytest.mark.parametrize("graph", [1, 2])
-def test_batch_broadphase_fused(ctx, stq, oracle, cuda, scenes, graph):
+@pytest.mark.parametrize("shape", [1, 2])
+def test_batch_broadphase_fused(ctx, stq, oracle, cuda, scenes, graph, shape):
     import torch
 
     meshes, want = scenes
     ctx.set_option(stq.OPT_GRAPH, graph)
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     V0, V1, E, F, vo, eo, fo = stq.concat_meshes(meshes)
     n = sum(m.num_boxes for m in meshes)
     bo = np.concatenate([[0], np.cumsum([m.num_boxes for m in meshes])])
@@ -194,8 +200,10 @@ def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes)
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
     ms, settings = ctx.autotune(boxes, bo, pairs, cap)
     assert ms > 0
-    assert settings["lanes"] in (1, 4, 8, 16) and settings["queue"] in (32, 64, 128)
+    assert settings["shape"] in (stq.SHAPE_QUEUE, stq.SHAPE_FLAT)
+    assert settings["lanes"] in (1, 4, 8, 16) and settings["queue"] in (16, 32, 64)
     assert settings["per_lane"] in (2, 4, 8) or settings["lanes"] > 1
+    assert settings["queue"] >= 32 or settings["lanes"] > 1
     assert settings["block"] in (128, 256, 512) and settings["radix_bits"] in (4, 8)
     assert settings["cell_scale"] in (1, 2, 4)
     r = ctx.sweep_prepared(pairs, cap)

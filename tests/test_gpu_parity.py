@@ -130,9 +130,11 @@ def test_sweep_cloth_pair_vs_oracle(ctx, stq, oracle, cuda, c0, axis):
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
-@pytest.mark.parametrize("queue", [32, 64, 128])
+@pytest.mark.parametrize("queue", [16, 32, 64, 128])
 @pytest.mark.parametrize("block", [128, 256, 512])
 def test_sweep_tuning_space(ctx, stq, oracle, cuda, c0, lanes, queue, block):
+    """Queue depth 16 holds one entry per lane group for groups of 2 or more
+    lanes; one start box per lane keeps a ring of at least 32."""
     m, boxes, want = c0
     ctx.set_option(stq.OPT_LANES, lanes)
     ctx.set_option(stq.OPT_QUEUE, queue)
@@ -156,13 +158,38 @@ def test_sweep_one_lane_per_box(ctx, stq, oracle, cuda, c0, per_lane, queue, blo
         assert np.array_equal(got, want), axis
 
 
+@pytest.mark.parametrize("steps", [2, 4])
+@pytest.mark.parametrize("block", [128, 256])
+def test_sweep_flat_shape(ctx, stq, oracle, cuda, c0, steps, block):
+    """The flat shape (runs of 32 start boxes laid end to end, one candidate
+    per lane and step, run ends from the gather) gives the oracle's pairs and
+    tests the same candidates as the queue shape."""
+    m, boxes, want = c0
+    sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
+    cand = ctx.candidates
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, stq.SHAPE_FLAT)
+    ctx.set_option(stq.OPT_PER_LANE, steps)
+    ctx.set_option(stq.OPT_BLOCK, block)
+    assert ctx.get_option(stq.OPT_SWEEP_SHAPE) == stq.SHAPE_FLAT
+    for axis in (0, -1, 1, 2):
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis)
+        assert np.array_equal(got, want), axis
+        if axis == 0:
+            assert ctx.candidates == cand
+    for cells in (1, 7):  # one cell; a fixed grid
+        ctx.set_option(stq.OPT_CELLS, cells)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1)
+        assert np.array_equal(got, want), cells
+
+
 @pytest.mark.parametrize("run_cap", [1, 5, 64])
-@pytest.mark.parametrize("shape", [(1, 4), (1, 8), (8, 0), (2, 0)])
+@pytest.mark.parametrize("shape", [(1, 4, 1), (1, 8, 1), (8, 0, 1), (2, 0, 1), (1, 2, 2), (1, 4, 2)])
 def test_long_runs_go_to_the_warp_pass(ctx, stq, oracle, cuda, c0, run_cap, shape):
     """Runs longer than the cap continue in the warp pass: same pairs, same
-    candidates tested as without the hand-over."""
+    candidates tested as without the hand-over (queue and flat shapes)."""
     m, boxes, want = c0
     ctx.set_option(stq.OPT_LANES, shape[0])
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape[2])
     if shape[1]:
         ctx.set_option(stq.OPT_PER_LANE, shape[1])
     ctx.set_option(stq.OPT_RUN_CAP, (1 << 20))
@@ -184,13 +211,15 @@ def dense_cloth(stq, oracle):
     return m, boxes, oracle.broadphase(boxes)
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("run_cap", [0, 16])
-def test_dense_scene_vs_oracle(ctx, stq, oracle, cuda, dense_cloth, run_cap):
+def test_dense_scene_vs_oracle(ctx, stq, oracle, cuda, dense_cloth, run_cap, shape):
     import torch
 
     m, boxes, want = dense_cloth
     assert len(want) > 40 * len(boxes)
     ctx.set_option(stq.OPT_RUN_CAP, run_cap)
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1, cap=len(want) + 8)
     assert np.array_equal(got, want)
     # overflow and resume: count mode adds the warp pass's counts
@@ -214,8 +243,10 @@ def test_sweep_radix_4bit(ctx, stq, oracle, cuda, c0):
     assert np.array_equal(sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 1), want)
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("seed", [3, 4])
-def test_sweep_skewed_boxes_vs_oracle(ctx, stq, oracle, cuda, seed):
+def test_sweep_skewed_boxes_vs_oracle(ctx, stq, oracle, cuda, seed, shape):
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     boxes = stq.random_boxes(200_000, sliver_frac=0.05, seed=seed)
     want = oracle.broadphase(boxes)
     for axis in (0, -1):
@@ -234,11 +265,13 @@ def test_sweep_ids_are_box_ids_not_positions(ctx, stq, oracle, cuda, c0):
 
 # ---- overflow and resume ---------------------------------------------------------------
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("div", [2, 7, 50])
-def test_overflow_resume_covers_everything_once(ctx, stq, oracle, cuda, c0, div):
+def test_overflow_resume_covers_everything_once(ctx, stq, oracle, cuda, c0, div, shape):
     import torch
 
     m, boxes, want = c0
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     cap = len(want) // div + 1
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=cuda)
     ctx.prepare(boxes_dev(boxes, cuda), len(boxes), 0)
@@ -487,8 +520,9 @@ def test_host_call_windows_match_device_sweep(stq, oracle, cuda, big_cloth, over
         assert np.array_equal(oracle.canonical(small[: rs.count]), oracle.canonical(dp[: ref.count].cpu().numpy()))
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("windows", [2, 3, 32])
-def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows):
+def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows, shape):
     """Any window count (odd counts end on the first slot; 32 is more than
     this scene's 2^19-position windows allow) gives the device sweep's pairs;
     a capacity that the first window alone exceeds gives the prefix rule's."""
@@ -507,6 +541,7 @@ def test_host_call_window_counts(stq, oracle, cuda, big_cloth, windows):
         want = oracle.canonical(dp[: r.count].cpu().numpy())
         ctx.set_option(stq.OPT_HOST_WINDOWS, windows)
         assert ctx.get_option(stq.OPT_HOST_WINDOWS) == windows
+        ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
         out = torch.empty((len(want), 2), dtype=torch.int32).pin_memory().numpy()
         ctx.set_option(stq.OPT_HOST_OVERLAP, 2)
         l0 = ctx.launches
@@ -663,8 +698,9 @@ def _f32_lower_bound(C, lo, inv):
     return ofloat(b)
 
 
+@pytest.mark.parametrize("shape", [1, 2])
 @pytest.mark.parametrize("lo,hi,n", [(0.0, 1.0, 8), (0.1, 0.8, 7), (-0.37, 1.91, 13), (1000.25, 1003.0, 11)])
-def test_first_cell_rule_at_cell_bounds(ctx, stq, oracle, cuda, lo, hi, n):
+def test_first_cell_rule_at_cell_bounds(ctx, stq, oracle, cuda, lo, hi, n, shape):
     """A pair found in several cells is emitted in the cell of its reference
     point, tested on the candidate's minima against the start box's cell lower
     bounds. Boxes whose minima sit one float below, on and one float above
@@ -699,6 +735,7 @@ def test_first_cell_rule_at_cell_bounds(ctx, stq, oracle, cuda, lo, hi, n):
     assert len(want) > len(boxes)
     ctx.set_option(stq.OPT_CELLS, n)
     ctx.set_option(stq.OPT_REPLICA_BUDGET, 64)
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
     got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, axis=0)
     assert ctx.list_stats()["lists"] == 3 * n * n  # the grid the host computed
     assert np.array_equal(got, want)

@@ -39,15 +39,40 @@ def test_each_timestep_is_exact(stq, oracle, cuda):
     assert want[0][0] > 0 and len(set(w[1] for w in want)) == 4  # the scene moved
 
 
-@pytest.mark.parametrize("shape", [(1, 8), (4, 0), (8, 0)])
+def test_large_request_each_timestep_is_exact(stq, oracle, cuda):
+    """A request of over a million boxes, batched with a small one: every
+    timestep's pair count and checksum equal the oracle's on the positions the
+    device used, and the request ran one step per tick."""
+    mesh = stq.cloth_pair(g=292, z_offset=0.004, sigma=0.004, seed=33)
+    assert mesh.num_boxes >= 1_000_000
+    small = stq.cloth_pair(g=20, z_offset=0.004, sigma=0.004, seed=34)
+    with stq.Server(0, None, budget_bytes=32 << 30, max_boxes=1 << 22, max_scenes=8) as sv:
+        other = sv.submit(small, steps=5, sigma=0.003, seed=1)
+        rid = sv.submit(mesh, steps=3, sigma=0.003, seed=78)
+        want = []
+        for step in range(3):
+            sv.tick()
+            V0, V1 = sv.mesh(rid)
+            want.append(oracle_step(stq, oracle, mesh, V0, V1))
+        run_until_done(sv, [rid, other])
+        counts, checks = sv.result(rid)
+        first, last = sv.request_ticks(rid)
+    assert [int(c) for c in counts] == [w[0] for w in want]
+    assert [int(c) for c in checks] == [w[1] for w in want]
+    assert want[0][0] > 1_000_000
+    assert first == 0 and last - first + 1 == 3
+
+
+@pytest.mark.parametrize("shape", [(1, 8, 1), (4, 0, 1), (8, 0, 1), (1, 4, 2), (1, 2, 2)])
 def test_server_sweep_shapes_agree(stq, cuda, shape):
     """stq_server_set_option retunes the server's sweep (the next tick captures
     again); every shape gives the same per-step counts and checksums."""
     mesh = stq.cloth_pair(g=60, z_offset=0.003, sigma=0.006, seed=8)
     results = []
-    for s in ((8, 0), shape):
+    for s in ((8, 0, 1), shape):
         with stq.Server(0, None, budget_bytes=8 << 30, max_boxes=1 << 20, max_scenes=8) as sv:
             sv.set_option(stq.OPT_LANES, s[0])
+            sv.set_option(stq.OPT_SWEEP_SHAPE, s[2])
             if s[1]:
                 sv.set_option(stq.OPT_PER_LANE, s[1])
             sv.set_option(stq.OPT_RUN_CAP, 4)  # the warp pass too

@@ -1,5 +1,7 @@
 """stq_sweep_static: the sweep for callers that cannot allocate device memory
-(stream capture, fixed up-front budgets, foreign allocators). It must return
+when they need a broad phase (steps under a memory budget reserved up front,
+hosts whose own pooling allocator owns the device memory, real-time loops that
+cannot take cudaFree's device-wide synchronisation). It must return
 exactly the pairs of the ordinary entry point stq_sweep, call after call,
 while using only the library's static scratch array.
 
