@@ -255,7 +255,21 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
             "tuned_prepare_sweep_ms": tune_ms}
 
 
-def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush):
+def context_options(stq, ctx, spec: str) -> dict:
+    """Applies `name=value,...` context options (cell_scale, shape, per_lane,
+    lanes, queue, block, radix_bits); returns them as a dict."""
+    names = {"cell_scale": stq.OPT_CELL_SCALE, "shape": stq.OPT_SWEEP_SHAPE, "per_lane": stq.OPT_PER_LANE,
+             "lanes": stq.OPT_LANES, "queue": stq.OPT_QUEUE, "block": stq.OPT_BLOCK,
+             "radix_bits": stq.OPT_RADIX_BITS}
+    out = {}
+    for item in filter(None, spec.split(",")):
+        k, v = item.split("=")
+        ctx.set_option(names[k], int(v))
+        out[k] = int(v)
+    return out
+
+
+def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush, tune=True, options=""):
     """64 scenes of 500,000 random boxes (95% small, lognormal extents around
     0.002; 5% slivers stretched 200x along a random axis), sweep axis x in half
     of the scenes and the largest-variance axis in the other half: the batched
@@ -276,6 +290,11 @@ def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush):
     total = ctx.sweep_prepared(pairs, cap).total
     cap = int(total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
+    # settings tuned on the same batch (untimed; the tuner prepares with the
+    # largest-variance axis in every scene, the timed runs use the axes above)
+    tuned = context_options(stq, ctx, options) or "library defaults"
+    if tune:
+        tune_ms, tuned = ctx.autotune(boxes, box_off, pairs, cap)
 
     def timed(fn):
         for _ in range(warmup):
@@ -309,7 +328,7 @@ def bench_skewed(stq, torch, dev, stream, local, steps, warmup, flush):
     ctx.close()
     n = len(allb)
     return {"workload": "64 x 500k random boxes, 5% slivers (200x), axis x / max-variance alternating",
-            "boxes": n, "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain,
+            "boxes": n, "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain, "tuned": tuned,
             "batched_boxes_per_s": n / (t_batch / 1e3), "batched_pairs_per_s": total / (t_batch / 1e3),
             "batched_over_plain": t_plain / t_batch}
 
@@ -469,6 +488,10 @@ def main():
                     help="skip the 8M-box scene and the skewed 64-scene batch")
     ap.add_argument("--no-tune", action="store_true",
                     help="skip the autotuner (use the library defaults), e.g. for profiling")
+    ap.add_argument("--options", type=str, default="",
+                    help="context options for the main scene, e.g. cell_scale=4,shape=2 (with --no-tune)")
+    ap.add_argument("--only-skewed", action="store_true",
+                    help="run the skewed 64-scene batch alone and print its figures (profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rates", type=str, default="50,200,500,1000,2000")
     args = ap.parse_args()
@@ -509,6 +532,11 @@ def main():
     boxes = torch.empty((n, 11), dtype=torch.int32, device=dev)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.int32, device=dev)
     torch.cuda.synchronize(dev)
+    if args.only_skewed:
+        if rank == 0:
+            print(json.dumps(bench_skewed(stq, torch, dev, stream, local, args.steps, args.warmup, flush,
+                                          tune=not args.no_tune, options=args.options)), flush=True)
+        return
 
     ctx = stq.Context(local, stream.cuda_stream)
     # size the pair buffer from a first run
@@ -519,9 +547,11 @@ def main():
     r = ctx.sweep_prepared(pairs, cap)
     cap = int(r.total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
-    # the project's autotuner picks cell scale, radix width, lane-group width,
-    # queue depth and block size for this workload (not timed)
-    tuned = "library defaults"
+    # the project's autotuner picks cell scale, radix width, sweep shape,
+    # lane-group width, queue depth and block size for this workload (not
+    # timed); --no-tune with --options name=value,... sets them by hand instead
+    # (profiling runs, which must not launch the tuner's trials)
+    tuned = context_options(stq, ctx, args.options) or "library defaults"
     if not args.no_tune:
         tune_ms, tuned = ctx.autotune(boxes, [0, n], pairs, cap)
 
@@ -644,6 +674,7 @@ def main():
                        "call": "stq_broadphase_host",
                        "pairs_out": "sweep windows, each copied while later ones are swept",
                        "ms_median": 1e3 * ts_sorted[len(ts) // 2], "ms_min": 1e3 * ts_sorted[0],
+                       "ms_steps": [round(1e3 * t, 3) for t in ts],
                        "one_copy_after_sweep_ms_per_step": 1e3 * sum(ts_staged) / len(ts_staged),
                        "link_alone_ms": {"h2d_mesh": h2d_ms, "d2h_pairs": d2h_ms,
                                          "d2h_gbs": 8 * npairs / d2h_ms / 1e6}}

@@ -1193,7 +1193,7 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   std::vector<int64_t> best_set(kOpts, 0);
   float best_total = 1e30f;
   int st = STQ_OK;
-  for (int64_t scale : {1, 2, 4}) {
+  for (int64_t scale : {1, 2, 4, 8}) {
     if ((st = stq_context_set_option(ctx, STQ_OPT_CELL_SCALE, scale)) != STQ_OK) break;
     // the radix width changes the prepare only: the sorted scene is the same
     float t_prep = 1e30f;

@@ -245,7 +245,11 @@ batch_policy_kernel(const stq_aabb *__restrict__ boxes, const long long *__restr
     if (!(w[1] > 0.f)) w[1] = Lc / 1024.f;
     nb = grid_side(Lb, r.cell_scale * w[0]);
     nc = grid_side(Lc, r.cell_scale * w[1]);
-    const long long max_cells = max(1ll, min(1ll << 20, n / 16));
+    // at least 8 * scale boxes per cell on average (16 at the default scale
+    // 2): dense scenes of small boxes would otherwise be cut into lists of a
+    // few boxes, and their prepare would outweigh the sweep
+    const long long per_cell = max(1ll, (long long)(8.f * r.cell_scale));
+    const long long max_cells = max(1ll, min(1ll << 20, n / per_cell));
     while ((long long)nb * nc > max_cells) {
       if (nb >= nc) nb = (nb + 1) / 2;
       else nc = (nc + 1) / 2;

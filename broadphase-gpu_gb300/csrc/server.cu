@@ -64,38 +64,77 @@ advance_kernel(const MeshRef *__restrict__ refs, const long long *__restrict__ v
 }
 
 // XOR over each scene's pairs of mix64((lo << 32) | hi), ids local to the
-// scene; each thread takes 32 consecutive pairs and flushes once per scene.
+// scene. A warp takes kChecksumChunk consecutive pairs, 32 per step (one per
+// lane, coalesced), and keeps the XOR of the current scene in its lanes'
+// registers. The pair list holds runs of one scene (each sweep warp appends
+// 32 or more pairs of consecutive start positions at once), so the warp
+// reduces its registers and flushes them with one atomic per run: at a scene
+// change inside a step, the lanes still in the old scene add to the registers
+// before the flush, and the lanes of the new scene after it. A lane whose pair
+// lies in a third scene within one step adds it alone.
+constexpr int kChecksumChunk = 1024;
+
+__device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, int S, long long id) {
+  int lo = 0, hi = S - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (box_off[mid] <= id) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
 __global__ void __launch_bounds__(256)
 pair_checksum_kernel(const int2 *__restrict__ pairs, long long capacity, const BatchHeader *hdr,
                      const long long *__restrict__ box_off, unsigned long long *checks) {
-  constexpr int kPer = 32;
   const long long n = min((long long)hdr->pairs, capacity);
   const int S = hdr->n_scenes;
-  for (long long base = (blockIdx.x * 256ll + threadIdx.x) * kPer; base < n;
-       base += (long long)gridDim.x * 256 * kPer) {
-    int cur = -1;
+  const int lane = threadIdx.x & 31;
+  const long long warp = (blockIdx.x * 256ll + threadIdx.x) >> 5;
+  const long long nwarps = (gridDim.x * 256ll) >> 5;
+  auto flush = [&](int cur, unsigned long long acc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0 && cur >= 0 && acc) atomicXor(&checks[cur], acc);
+  };
+  for (long long base = warp * kChecksumChunk; base < n; base += nwarps * kChecksumChunk) {
+    const long long end = min(base + kChecksumChunk, n);
+    int cur = -1;  // warp-uniform: scene of the registers' XOR
     long long b0 = 0, b1 = 0;
     unsigned long long acc = 0;
-    const long long end = min(base + kPer, n);
-    for (long long q = base; q < end; ++q) {
-      const int2 p = pairs[q];
-      if (cur < 0 || p.x < b0 || p.x >= b1) {
-        if (cur >= 0 && acc) atomicXor(&checks[cur], acc);
-        int lo = 0, hi = S - 1;
-        while (lo < hi) {
-          const int mid = (lo + hi + 1) >> 1;
-          if (box_off[mid] <= p.x) lo = mid;
-          else hi = mid - 1;
-        }
-        cur = lo;
-        b0 = box_off[lo];
-        b1 = box_off[lo + 1];
-        acc = 0;
+    for (long long q0 = base; q0 < end; q0 += 32) {
+      const long long q = q0 + lane;
+      const bool valid = q < end;
+      int2 p = make_int2(0, 0);
+      if (valid) p = pairs[q];
+      const bool in = valid && p.x >= b0 && p.x < b1;
+      if (in) {
+        const unsigned long long a = (unsigned long long)(p.x - b0), c = (unsigned long long)(p.y - b0);
+        acc ^= mix64((a << 32) | c);
       }
-      const unsigned long long a = (unsigned long long)(p.x - b0), c = (unsigned long long)(p.y - b0);
-      acc ^= mix64((a << 32) | c);
+      const unsigned outm = __ballot_sync(0xffffffffu, valid && !in);
+      if (outm) {
+        // the scene changes: flush, and take the scene of the first lane outside
+        flush(cur, acc);
+        acc = 0;
+        const int leader = __ffs(outm) - 1;
+        int s = 0;
+        if (lane == leader) s = scene_of(box_off, S, p.x);
+        cur = __shfl_sync(0xffffffffu, s, leader);
+        b0 = box_off[cur];
+        b1 = box_off[cur + 1];
+        if (valid && !in) {
+          const bool in_new = p.x >= b0 && p.x < b1;
+          const int t = in_new ? cur : scene_of(box_off, S, p.x);
+          const unsigned long long a = (unsigned long long)(p.x - box_off[t]),
+                                   c = (unsigned long long)(p.y - box_off[t]);
+          const unsigned long long h = mix64((a << 32) | c);
+          if (in_new) acc ^= h;
+          else atomicXor(&checks[t], h);
+        }
+      }
     }
-    if (cur >= 0 && acc) atomicXor(&checks[cur], acc);
+    flush(cur, acc);
   }
 }
 
@@ -114,7 +153,7 @@ cudaError_t launch_pair_checksums(cudaStream_t s, const stq_pair *pairs, long lo
                                   unsigned long long *checks, int scene_cap) {
   cudaError_t e = cudaMemsetAsync(checks, 0, sizeof(unsigned long long) * size_t(scene_cap), s);
   if (e != cudaSuccess) return e;
-  int64_t g = (capacity / 32 + 255) / 256;
+  int64_t g = (capacity / kChecksumChunk + 7) / 8;  // 8 warps per block
   g = g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
   pair_checksum_kernel<<<unsigned(g), 256, 0, s>>>(reinterpret_cast<const int2 *>(pairs), capacity,
                                                    hdr, box_off, checks);
@@ -344,9 +383,12 @@ int stq_server_create(int device, void *stream, int64_t budget_bytes, int64_t ma
   int st = stq_context_create(device, stream, &sv->ctx);
   if (st != STQ_OK) return st;
   stq_context *ctx = sv->ctx;
-  // serving batches of many dense scenes sweep fastest with lane groups of 8
-  // sharing a start box (measured); stq_server_set_option changes it
-  stq_context_set_option(ctx, STQ_OPT_LANES_PER_ENTRY, 8);
+  // serving batches of many dense time-stepped scenes sweep fastest in the
+  // flat shape with four filter steps per round (measured on 24 cloth-pair
+  // requests: 47 ms per tick against 66 ms for lane groups of 8);
+  // stq_server_set_option changes it
+  stq_context_set_option(ctx, STQ_OPT_SWEEP_SHAPE, kShapeFlat);
+  stq_context_set_option(ctx, STQ_OPT_CANDIDATES_PER_LANE, 4);
   stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, 256);
   DeviceGuard g(device);
   sv->device = device;

@@ -140,7 +140,7 @@ constexpr int kShapeFlat = 2;
 
 // Sweep-kernel tuning (autotuned or set through stq_context_set_option).
 struct SweepTuning {
-  int shape = kShapeRing;  // kShapeRing or kShapeFlat
+  int shape = kShapeFlat;  // kShapeFlat or kShapeRing
   int lanes = 1;        // lanes sharing one pending start box (1..32)
   int per_lane = 8;     // lanes = 1: candidates a lane tests per step (1, 2, 4, 8)
   int run_cap = 512;    // candidates per start box before the warp pass takes over

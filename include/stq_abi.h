@@ -82,8 +82,8 @@ enum { STQ_AXIS_AUTO = -1, STQ_AXIS_X = 0, STQ_AXIS_Y = 1, STQ_AXIS_Z = 2 };
 
 /* Tuning knobs for stq_context_set_option (0 restores the automatic choice). */
 typedef enum stq_option {
-  STQ_OPT_LANES_PER_ENTRY = 1, /* lanes that share one queue entry: 1 (default),
-                                  2, 4, 8, 16, 32                                   */
+  STQ_OPT_LANES_PER_ENTRY = 1, /* queue shape: lanes that share one queue entry:
+                                  1 (default), 2, 4, 8, 16, 32                      */
   STQ_OPT_QUEUE_DEPTH = 2,     /* entries per warp queue: 16, 32, 64 (default) or
                                   128; with one lane per entry the queue holds at
                                   least 32 (16 acts as 32)                         */
@@ -92,7 +92,8 @@ typedef enum stq_option {
                                   1 no cells (plain sweep), k > 1 a k x k grid      */
   STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
   STQ_OPT_CELL_SCALE = 6,      /* automatic cell side in median box extents (1..64,
-                                  default 2)                                        */
+                                  default 2); a scene of n boxes gets at most
+                                  n / (8 * scale) cells                             */
   STQ_OPT_REPLICA_BUDGET = 7,  /* cell replicas per box a scene may use (1..64,
                                   default 4); finer grids beyond it are coarsened   */
   STQ_OPT_GRAPH = 8,           /* stq_batch_broadphase: 1 capture and replay a CUDA
@@ -111,13 +112,12 @@ typedef enum stq_option {
   STQ_OPT_HOST_WINDOWS = 12,   /* stq_sweep_host / stq_broadphase_host: windows a
                                   sweep is cut into (2..32, default 16; fewer when
                                   the scene has under 2^19 positions per window) */
-  STQ_OPT_SWEEP_SHAPE = 13     /* 1 (default): a per-warp queue of pending start
-                                  boxes taken by lanes or lane groups
-                                  (STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH);
-                                  2: flat, each warp lays the runs of 32 start
-                                  boxes end to end and tests one candidate per
-                                  lane and step (block size 128 or 256; 512 acts
-                                  as 256)                                          */
+  STQ_OPT_SWEEP_SHAPE = 13     /* 2 (default): flat, each warp lays the runs of 32
+                                  start boxes end to end and tests one candidate
+                                  per lane and step (block size 128 or 256; 512
+                                  acts as 256); 1: a per-warp queue of pending
+                                  start boxes taken by lanes or lane groups
+                                  (STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH)  */
 } stq_option;
 
 typedef struct stq_context stq_context;
@@ -270,7 +270,7 @@ int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count);
 /* ---- autotuning --------------------------------------------------------------
  * Times prepare + sweep of the given batch (as stq_batch_prepare, all start
  * boxes), each setting five times (the fastest counts), over cell scale
- * {1, 2, 4} and radix digit width {4, 8} (the prepare), and over the sweep
+ * {1, 2, 4, 8} and radix digit width {4, 8} (the prepare), and over the sweep
  * shapes (the work split of the start boxes' runs): one start box per lane
  * with 2, 4 or 8 candidates per step (queue depth {32, 64}), lane groups of
  * 4, 8 or 16 lanes (queue depth {16, 32, 64}), each with block size

@@ -205,7 +205,7 @@ def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes)
     assert settings["per_lane"] in (2, 4, 8) or settings["lanes"] > 1
     assert settings["queue"] >= 32 or settings["lanes"] > 1
     assert settings["block"] in (128, 256, 512) and settings["radix_bits"] in (4, 8)
-    assert settings["cell_scale"] in (1, 2, 4)
+    assert settings["cell_scale"] in (1, 2, 4, 8)
     r = ctx.sweep_prepared(pairs, cap)
     check_batch(oracle, pairs[: r.count].cpu().numpy(), bo, want, ctx.batch_scene_pairs(len(meshes)))
     ms2, settings2 = ctx.autotune(boxes, bo, pairs, cap)  # same shape bucket: cached

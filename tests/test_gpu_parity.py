@@ -136,6 +136,7 @@ def test_sweep_tuning_space(ctx, stq, oracle, cuda, c0, lanes, queue, block):
     """Queue depth 16 holds one entry per lane group for groups of 2 or more
     lanes; one start box per lane keeps a ring of at least 32."""
     m, boxes, want = c0
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, stq.SHAPE_QUEUE)
     ctx.set_option(stq.OPT_LANES, lanes)
     ctx.set_option(stq.OPT_QUEUE, queue)
     ctx.set_option(stq.OPT_BLOCK, block)
@@ -148,6 +149,7 @@ def test_sweep_tuning_space(ctx, stq, oracle, cuda, c0, lanes, queue, block):
 @pytest.mark.parametrize("block", [128, 512])
 def test_sweep_one_lane_per_box(ctx, stq, oracle, cuda, c0, per_lane, queue, block):
     m, boxes, want = c0
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, stq.SHAPE_QUEUE)
     ctx.set_option(stq.OPT_LANES, 1)
     ctx.set_option(stq.OPT_PER_LANE, per_lane)
     ctx.set_option(stq.OPT_QUEUE, queue)
@@ -165,6 +167,7 @@ def test_sweep_flat_shape(ctx, stq, oracle, cuda, c0, steps, block):
     per lane and step, run ends from the gather) gives the oracle's pairs and
     tests the same candidates as the queue shape."""
     m, boxes, want = c0
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, stq.SHAPE_QUEUE)
     sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, 0)
     cand = ctx.candidates
     ctx.set_option(stq.OPT_SWEEP_SHAPE, stq.SHAPE_FLAT)
