@@ -467,7 +467,7 @@ void stq_context_destroy(stq_context *ctx) {
     if (ctx->graph_stream) cudaStreamDestroy(ctx->graph_stream);
     if (ctx->graph_event) cudaEventDestroy(ctx->graph_event);
     if (ctx->owns_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
-    for (DevBuf *b : {&ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts, &ctx->box_cells,
+    for (DevBuf *b : {&ctx->points, &ctx->in_dev, &ctx->scenes, &ctx->cell_base, &ctx->scene_pairs, &ctx->counts, &ctx->box_cells,
                       &ctx->offsets, &ctx->scan_ws, &ctx->keys64[0], &ctx->keys64[1], &ctx->vals[0],
                       &ctx->vals[1], &ctx->sort_ws, &ctx->xmin, &ctx->xmax, &ctx->syz, &ctx->sv, &ctx->sflag, &ctx->sfloor, &ctx->cell_floor, &ctx->partner, &ctx->run_end, &ctx->long_list,
                       &ctx->seg_scan, &ctx->bkeys[0], &ctx->bkeys[1],
@@ -613,12 +613,15 @@ int stq_build_boxes(stq_context *ctx, const double *d_V0, const double *d_V1, in
   DeviceGuard g(ctx->device);
   BatchHeader *aux = ctx->aux.as<BatchHeader>();
   STQ_CUDA(ctx, cudaMemsetAsync(aux, 0, sizeof(BatchHeader), ctx->stream), "clear flags");
+  STQ_CUDA(ctx, ctx->points.ensure(2 * sizeof(float4) * size_t(std::max<int64_t>(nV, 1))),
+           "allocate rounded positions");
   stage_begin(ctx, kBuild);
   STQ_CUDA(ctx, launch_build_boxes(ctx->stream, d_V0, d_V1, nV, d_E, nE, d_F, nF,
-                                   ref_next_up(inflation_radius), d_boxes, &aux->flags),
+                                   ref_next_up(inflation_radius), d_boxes, &aux->flags,
+                                   ctx->points.as<float4>()),
            "launch box build");
   stage_end(ctx, kBuild);
-  ctx->launches += 1;
+  ctx->launches += nV > 0 ? 2 : 1;
   return read_header(ctx, aux);
 }
 
@@ -647,15 +650,19 @@ int stq_batch_build_boxes(stq_context *ctx, const double *d_V0, const double *d_
   fill_staging(ctx, box_off.data(), n_scenes, nullptr, STQ_AXIS_AUTO, h_vert_off, h_edge_off,
                h_face_off);
   STQ_TRY(upload_staging(ctx));
+  const int64_t nv_all = h_vert_off[n_scenes];
+  STQ_CUDA(ctx, ctx->points.ensure(2 * sizeof(float4) * size_t(std::max<int64_t>(nv_all, 1))),
+           "allocate rounded positions");
   stage_begin(ctx, kBuild);
   STQ_CUDA(ctx, launch_batch_build(ctx->stream, d_V0, d_V1, dev_at<long long>(ctx, ctx->layout.voff),
                                    d_E, dev_at<long long>(ctx, ctx->layout.eoff), d_F,
                                    dev_at<long long>(ctx, ctx->layout.foff),
                                    dev_at<long long>(ctx, ctx->layout.box_off), dev_hdr(ctx), N,
-                                   ref_next_up(inflation_radius), d_boxes),
+                                   ref_next_up(inflation_radius), d_boxes, ctx->points.as<float4>(),
+                                   std::max<int64_t>(nv_all, 1)),
            "launch batched box build");
   stage_end(ctx, kBuild);
-  ctx->launches += 1;
+  ctx->launches += 2;
   return read_header(ctx);
 }
 
@@ -804,6 +811,10 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
   STQ_TRY(ensure_replica_buffers(ctx, rep_cap, cells_cap));
   STQ_CUDA(ctx, ctx->batch_boxes.ensure(sizeof(stq_aabb) * size_t(std::max<int64_t>(N, 1))),
            "allocate batch boxes");
+  // the rounded positions: a graph replays for any batch whose vertices fit
+  STQ_CUDA(ctx, ctx->points.ensure(2 * sizeof(float4) * size_t(std::max<int64_t>(h_vert_off[n_scenes], 1))),
+           "allocate rounded positions");
+  const int64_t vert_cap = int64_t(ctx->points.bytes / (2 * sizeof(float4)));
   fill_staging(ctx, box_off.data(), n_scenes, nullptr, axis, h_vert_off, h_edge_off, h_face_off);
   const stq_aabb *boxes = ctx->batch_boxes.as<stq_aabb>();
   const int cell_bits = bits_for(3 * cells_cap);
@@ -815,8 +826,9 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
                                      dev_at<long long>(ctx, ctx->layout.foff),
                                      dev_at<long long>(ctx, ctx->layout.box_off), dev_hdr(ctx),
                                      ctx->box_cap, ref_next_up(inflation_radius),
-                                     ctx->batch_boxes.as<stq_aabb>()),
+                                     ctx->batch_boxes.as<stq_aabb>(), ctx->points.as<float4>(), vert_cap),
              "launch batched box build");
+    ctx->launches += 1;  // the rounding of the positions
     stage_end(ctx, kBuild);
     const BatchBuffers b = batch_buffers(ctx, boxes);
     STQ_TRY(enqueue_prepare_front(ctx, b, -1));
@@ -846,13 +858,14 @@ int stq_batch_broadphase(stq_context *ctx, const double *d_V0, const double *d_V
     cudaStream_t caller = ctx->stream;
     ctx->stream = ctx->graph_stream;
     GraphKey key;
-    const void *ptrs[6] = {d_V0, d_V1, d_E, d_F, d_pairs, boxes};
+    const void *ptrs[7] = {d_V0, d_V1, d_E, d_F, d_pairs, boxes, ctx->points.ptr};
     std::memcpy(key.ptr, ptrs, sizeof ptrs);
-    const int64_t sizes[8] = {ctx->box_cap, ctx->rep_cap, ctx->slot_cap, ctx->scene_cap,
-                              ctx->tile_cap, capacity, n_scenes, cell_bits};
+    const int64_t sizes[9] = {ctx->box_cap, ctx->rep_cap, ctx->slot_cap, ctx->scene_cap,
+                              ctx->tile_cap, capacity, n_scenes, cell_bits, vert_cap};
     std::memcpy(key.sizes, sizes, sizeof sizes);
-    for (int o = 0; o < 9; ++o) key.opts[o] = ctx->options[o];
-    key.opts[9] = int64_t(inflation_radius * 1e9f);
+    static_assert(sizeof(ctx->options) / sizeof(ctx->options[0]) == 16, "options in the graph key");
+    for (int o = 0; o < 16; ++o) key.opts[o] = ctx->options[o];
+    key.opts[16] = int64_t(inflation_radius * 1e9f);
     key.stream = caller;
     int st = STQ_OK;
     if (!ctx->graph || !(key == ctx->graph_key)) {

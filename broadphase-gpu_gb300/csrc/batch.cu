@@ -176,7 +176,7 @@ __device__ __forceinline__ int level_side(int base, int level) {
 // Sweep axis of largest corner variance (x, then y, preferred on ties, as
 // src/simulation.cu:630-635) unless fixed; level-0 cell side = cell_scale x
 // median box extent (from a strided sample of the scene's boxes), at most
-// 2048 cells per axis and at most max(1, n / 16) cells.
+// 2048 cells per axis and at most max(1, n / max(16, 8 x cell_scale)) cells.
 __global__ void __launch_bounds__(kBlock)
 batch_policy_kernel(const stq_aabb *__restrict__ boxes, const long long *__restrict__ box_off,
                     SceneRecord *scenes, BatchHeader *hdr) {
@@ -245,10 +245,10 @@ batch_policy_kernel(const stq_aabb *__restrict__ boxes, const long long *__restr
     if (!(w[1] > 0.f)) w[1] = Lc / 1024.f;
     nb = grid_side(Lb, r.cell_scale * w[0]);
     nc = grid_side(Lc, r.cell_scale * w[1]);
-    // at least 8 * scale boxes per cell on average (16 at the default scale
-    // 2): dense scenes of small boxes would otherwise be cut into lists of a
-    // few boxes, and their prepare would outweigh the sweep
-    const long long per_cell = max(1ll, (long long)(8.f * r.cell_scale));
+    // at least max(16, 8 * scale) boxes per cell on average: dense scenes of
+    // small boxes would otherwise be cut into lists of a few boxes, and their
+    // prepare would outweigh the sweep (the buffers are sized for n / 16 cells)
+    const long long per_cell = max(16ll, (long long)(8.f * r.cell_scale));
     const long long max_cells = max(1ll, min(1ll << 20, n / per_cell));
     while ((long long)nb * nc > max_cells) {
       if (nb >= nc) nb = (nb + 1) / 2;

@@ -44,9 +44,9 @@ struct Staging {
 };
 
 struct GraphKey {
-  const void *ptr[6] = {};
-  int64_t sizes[8] = {};
-  int64_t opts[10] = {};
+  const void *ptr[7] = {};
+  int64_t sizes[9] = {};
+  int64_t opts[17] = {};  // every context option, then the inflation radius
   cudaStream_t stream = nullptr;
   bool operator==(const GraphKey &o) const {
     return std::memcmp(ptr, o.ptr, sizeof ptr) == 0 && std::memcmp(sizes, o.sizes, sizeof sizes) == 0 &&
@@ -74,6 +74,7 @@ struct stq_context {
   char *in_host = nullptr;
   size_t in_host_bytes = 0;
   DevBuf scenes, cell_base, scene_pairs, counts, offsets, box_cells, scan_ws, keys64[2], vals[2], sort_ws;
+  DevBuf points;  // fp64 vertex positions rounded to float once (box builds)
   DevBuf xmin, xmax, syz, sv, sflag, sfloor, partner, run_end, box_counts, prefix_ws, pair_keys[2];
   DevBuf cell_floor;  // lower bounds of each cell on b and c
   DevBuf long_list;  // runs handed from the lane sweep to the warp pass

@@ -215,10 +215,11 @@ struct SweepParams {
 };
 
 // ---- launch wrappers (each returns the launch error) -------------------------
+// points: 2 * nV float4 of scratch for the rounded positions
 cudaError_t launch_build_boxes(cudaStream_t s, const double *V0, const double *V1,
                                int64_t nV, const int32_t *E, int64_t nE,
                                const int32_t *F, int64_t nF, float r_up,
-                               stq_aabb *out, int *flags);
+                               stq_aabb *out, int *flags, float4 *points);
 
 // ---- batch prepare (scene table) ---------------------------------------------------
 // Buffers sized by host capacities; actual sizes come from the BatchHeader.
@@ -268,10 +269,12 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 SortedScene scene);
 // Batched box build: scene s has vertices [voff[s], voff[s+1]) etc.; box ids
 // are global (box_off[s] + local), vertex ids local to the scene.
+// points: 2 * vert_cap float4 of scratch for the rounded positions
 cudaError_t launch_batch_build(cudaStream_t s, const double *V0, const double *V1,
                                const long long *voff, const int32_t *E, const long long *eoff,
                                const int32_t *F, const long long *foff, const long long *box_off,
-                               BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out);
+                               BatchHeader *hdr, int64_t box_cap, float r_up, stq_aabb *out,
+                               float4 *points, int64_t vert_cap);
 // A scene held by the serving loop: its own device mesh and time-step state.
 struct MeshRef {
   double *V0, *V1;

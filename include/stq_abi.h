@@ -93,7 +93,7 @@ typedef enum stq_option {
   STQ_OPT_RADIX_BITS = 5,      /* radix digit width: 4 or 8 (single-cell sort)     */
   STQ_OPT_CELL_SCALE = 6,      /* automatic cell side in median box extents (1..64,
                                   default 2); a scene of n boxes gets at most
-                                  n / (8 * scale) cells                             */
+                                  n / max(16, 8 * scale) cells                      */
   STQ_OPT_REPLICA_BUDGET = 7,  /* cell replicas per box a scene may use (1..64,
                                   default 4); finer grids beyond it are coarsened   */
   STQ_OPT_GRAPH = 8,           /* stq_batch_broadphase: 1 capture and replay a CUDA
