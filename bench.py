@@ -481,6 +481,8 @@ def main():
     ap.add_argument("--ref-step-s", type=float, default=3.0,
                     help="seconds of CPU sweep per step of the reference arm")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the check of the main scene's pairs against the CPU oracle")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
@@ -692,11 +694,26 @@ def main():
         line["serve"] = bench_serving(stq, local, args.serve_requests,
                                       [float(x) for x in args.serve_rates.split(",")])
 
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world == 1 and not (args.no_cpu_baseline and args.no_parity):
         orc = entry.load_oracle()
         hb = orc.construct_boxes(mesh.V0, mesh.V1, mesh.E, mesh.F, stq.AABB_DTYPE)
-        cb = cpu_sample_steps(orc, hb, pick_stride(orc, hb, args.cpu_step_s), args.cpu_steps, 1)
-        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        if not args.no_parity:
+            # the timed step's output against the oracle (after all timing):
+            # box bytes, and the whole sorted pair list
+            step()
+            ctx.sort_pairs(pairs, npairs)
+            got = pairs[:npairs].cpu().numpy()
+            t0 = time.perf_counter()
+            want = orc.broadphase(hb)
+            oracle_s = time.perf_counter() - t0
+            line["parity"] = {"checked": "box bytes and the sorted pair list of one step against the CPU oracle",
+                              "boxes_equal": boxes.cpu().numpy().tobytes() == hb.tobytes(),
+                              "pairs_equal": bool(got.shape == want.shape and np.array_equal(got, want)),
+                              "pairs": int(want.shape[0]), "oracle_s": oracle_s}
+            del got, want
+        if not args.no_cpu_baseline:
+            cb = cpu_sample_steps(orc, hb, pick_stride(orc, hb, args.cpu_step_s), args.cpu_steps, 1)
+            line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
     ctx.close()
     if dist:
         dist.destroy_process_group()
