@@ -260,7 +260,7 @@ def context_options(stq, ctx, spec: str) -> dict:
     lanes, queue, block, radix_bits); returns them as a dict."""
     names = {"cell_scale": stq.OPT_CELL_SCALE, "shape": stq.OPT_SWEEP_SHAPE, "per_lane": stq.OPT_PER_LANE,
              "lanes": stq.OPT_LANES, "queue": stq.OPT_QUEUE, "block": stq.OPT_BLOCK,
-             "radix_bits": stq.OPT_RADIX_BITS}
+             "radix_bits": stq.OPT_RADIX_BITS, "run_cap": stq.OPT_RUN_CAP}
     out = {}
     for item in filter(None, spec.split(",")):
         k, v = item.split("=")

@@ -1159,10 +1159,10 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
   *best_ms = 0.0;
   const int64_t key = (int64_t(bits_for(std::max<int64_t>(h_box_off[n_scenes], 1))) << 32) |
                       int64_t(bits_for(n_scenes));
-  constexpr int kOpts = 7;
+  constexpr int kOpts = 8;
   const int opts[kOpts] = {STQ_OPT_LANES_PER_ENTRY, STQ_OPT_QUEUE_DEPTH, STQ_OPT_BLOCK_SIZE,
                            STQ_OPT_RADIX_BITS, STQ_OPT_CELL_SCALE, STQ_OPT_CANDIDATES_PER_LANE,
-                           STQ_OPT_SWEEP_SHAPE};
+                           STQ_OPT_SWEEP_SHAPE, STQ_OPT_RUN_CAP};
   for (const auto &kv : ctx->tuned)
     if (kv.first == key) {
       for (int o = 0; o < kOpts; ++o) STQ_TRY(stq_context_set_option(ctx, opts[o], kv.second[size_t(o)]));
@@ -1190,19 +1190,21 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
     return STQ_OK;
   };
   // a sweep setting: shape, lanes per entry, candidates per lane (or filter
-  // steps of the flat shape), queue depth, block size
+  // steps of the flat shape), queue depth, block size, and the run length past
+  // which the warp pass takes a run over (the work split; 512 by default)
   struct Shape {
-    int64_t shape, lanes, per_lane, queue, block;
+    int64_t shape, lanes, per_lane, queue, block, run_cap;
   };
   std::vector<Shape> space;
   for (int64_t per_lane : {2, 4, 8})  // one start box per lane: the ring holds >= 32
     for (int64_t queue : {32, 64})
-      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, 1, per_lane, queue, block});
+      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, 1, per_lane, queue, block, 512});
   for (int64_t lanes : {4, 8, 16})  // lane groups sharing a start box
     for (int64_t queue : {16, 32, 64})
-      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, lanes, 8, queue, block});
+      for (int64_t block : {128, 256, 512}) space.push_back({kShapeRing, lanes, 8, queue, block, 512});
   for (int64_t steps : {2, 4})  // flat: runs of 32 start boxes end to end
-    for (int64_t block : {128, 256}) space.push_back({kShapeFlat, 1, steps, 64, block});
+    for (int64_t block : {128, 256})
+      for (int64_t run_cap : {512, 4096}) space.push_back({kShapeFlat, 1, steps, 64, block, run_cap});
   std::vector<int64_t> best_set(kOpts, 0);
   float best_total = 1e30f;
   int st = STQ_OK;
@@ -1229,6 +1231,7 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
       stq_context_set_option(ctx, STQ_OPT_CANDIDATES_PER_LANE, sh.per_lane);
       stq_context_set_option(ctx, STQ_OPT_QUEUE_DEPTH, sh.queue);
       stq_context_set_option(ctx, STQ_OPT_BLOCK_SIZE, sh.block);
+      stq_context_set_option(ctx, STQ_OPT_RUN_CAP, sh.run_cap);
       float t_sweep = 0.f;
       int64_t count = 0, next = 0, total = 0;
       st = elapsed([&] {
@@ -1238,7 +1241,7 @@ int stq_autotune(stq_context *ctx, const stq_aabb *d_boxes, const int64_t *h_box
       if (st != STQ_OK) break;
       if (t_prep + t_sweep < best_total) {
         best_total = t_prep + t_sweep;
-        best_set = {sh.lanes, sh.queue, sh.block, best_radix, scale, sh.per_lane, sh.shape};
+        best_set = {sh.lanes, sh.queue, sh.block, best_radix, scale, sh.per_lane, sh.shape, sh.run_cap};
       }
     }
     if (st != STQ_OK) break;

@@ -322,7 +322,8 @@ class Context:
         self._check(self.lib.stq_autotune(self._h, _ptr(boxes), bo.ctypes.data, len(bo) - 1, _ptr(pairs),
                                           capacity, ctypes.byref(ms)))
         names = {OPT_LANES: "lanes", OPT_QUEUE: "queue", OPT_BLOCK: "block", OPT_RADIX_BITS: "radix_bits",
-                 OPT_CELL_SCALE: "cell_scale", OPT_PER_LANE: "per_lane", OPT_SWEEP_SHAPE: "shape"}
+                 OPT_CELL_SCALE: "cell_scale", OPT_PER_LANE: "per_lane", OPT_SWEEP_SHAPE: "shape",
+                 OPT_RUN_CAP: "run_cap"}
         return ms.value, {v: self.get_option(k) for k, v in names.items()}
 
     def batch_scene_pairs(self, n_scenes: int) -> np.ndarray:

@@ -274,10 +274,12 @@ int stq_sort_pairs(stq_context *ctx, stq_pair *d_pairs, int64_t count);
  * shapes (the work split of the start boxes' runs): one start box per lane
  * with 2, 4 or 8 candidates per step (queue depth {32, 64}), lane groups of
  * 4, 8 or 16 lanes (queue depth {16, 32, 64}), each with block size
- * {128, 256, 512}, and the flat shape with 2 or 4 filter steps per round and
- * block size {128, 256}. Keeps the fastest prepare + sweep as the context's
- * options (cell scale, radix width, sweep shape, lanes per entry, candidates
- * per lane, queue depth, block size). Settings are cached per shape bucket
+ * {128, 256, 512}, and the flat shape with 2 or 4 filter steps per round,
+ * block size {128, 256} and run cap {512, 4096} (the run length past which the
+ * warp pass takes a run over). Keeps the fastest prepare + sweep as the
+ * context's options (cell scale, radix width, sweep shape, lanes per entry,
+ * candidates per lane, queue depth, block size, run cap). Settings are cached
+ * per shape bucket
  * (log2 of the box count, log2 of the scene count): a later call whose batch
  * falls in a tuned bucket applies them without timing. *best_ms receives the
  * prepare + sweep time of the chosen settings (0 on a cache hit). The batch is

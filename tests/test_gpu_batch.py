@@ -204,6 +204,7 @@ def test_autotune_keeps_results_exact_and_caches(ctx, stq, oracle, cuda, scenes)
     assert settings["lanes"] in (1, 4, 8, 16) and settings["queue"] in (16, 32, 64)
     assert settings["per_lane"] in (2, 4, 8) or settings["lanes"] > 1
     assert settings["queue"] >= 32 or settings["lanes"] > 1
+    assert settings["run_cap"] in (512, 4096)
     assert settings["block"] in (128, 256, 512) and settings["radix_bits"] in (4, 8)
     assert settings["cell_scale"] in (1, 2, 4, 8)
     r = ctx.sweep_prepared(pairs, cap)
