@@ -6,16 +6,22 @@
 // is_valid_pair (src/collision.cu:38-48, src/aabb.cu:33-40) and add_overlap
 // (src/collision.cu:50-74).
 //
-// GB300 design. Each warp owns a shared-memory ring of pending start boxes
-// (the "tiniest queue"). The warp is split into lane groups of G lanes; a
-// group takes one start box k from the ring and walks its x-run
-// j = partner[k], partner[k]+1, ... G candidates per step, until the first j
-// whose min exceeds k's max (a NaN sentinel ends every run). partner[k] is
-// k+1 for an edge, and the first face (for a vertex) or vertex (for a face)
-// of the same cell's list at or after k's min. A group that finishes
-// takes the next pending box, so a long run never stalls the other groups.
-// Refill, hand-out and pair output use __ballot_sync/__popc compaction: no
-// shared-memory atomics, and one global atomic per warp step that emits.
+// GB300 design. A start box k's candidates are its x-run
+// j = partner[k], partner[k]+1, ... up to the first j whose min exceeds k's
+// max (a NaN sentinel ends every list); partner[k] is k+1 for an edge, and the
+// first face (for a vertex) or vertex (for a face) of the same cell's list at
+// or after k's min. Two shapes walk the runs:
+//   - queue (stq_sweep_lane_kernel, stq_sweep_kernel): each warp owns a
+//     shared-memory ring of pending start boxes (the "tiniest queue"); a lane,
+//     or a group of G lanes, takes one start box from the ring and walks its
+//     run, and takes the next pending box when the run ends, so a long run
+//     never stalls the others;
+//   - flat (stq_sweep_flat_kernel, the default): the gather has found every
+//     run's end (run_end), so a warp lays the runs of 32 consecutive start
+//     positions end to end and tests one candidate per lane and step.
+// Runs longer than a cap go to a warp pass (stq_long_run_kernel). Refill,
+// hand-out and pair output use __ballot_sync/__popc compaction: no
+// shared-memory atomics, and one global atomic per 32 or more pairs.
 #include <map>
 #include <mutex>
 #include <type_traits>
