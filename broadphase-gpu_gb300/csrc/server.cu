@@ -71,8 +71,12 @@ advance_kernel(const MeshRef *__restrict__ refs, const long long *__restrict__ v
 // reduces its registers and flushes them with one atomic per run: at a scene
 // change inside a step, the lanes still in the old scene add to the registers
 // before the flush, and the lanes of the new scene after it. A lane whose pair
-// lies in a third scene within one step adds it alone.
+// lies in a third scene within one step adds it alone. Those XORs go to a
+// per-block table of the scenes in shared memory when it fits (SMEM), and the
+// block adds its table to the scenes' checksums once at the end: millions of
+// runs would otherwise contend on a few dozen global addresses.
 constexpr int kChecksumChunk = 1024;
+constexpr int kChecksumSmemScenes = 4096;  // 32 KB of shared memory
 
 __device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, int S, long long id) {
   int lo = 0, hi = S - 1;
@@ -84,18 +88,25 @@ __device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, i
   return lo;
 }
 
+template <bool SMEM>
 __global__ void __launch_bounds__(256)
 pair_checksum_kernel(const int2 *__restrict__ pairs, long long capacity, const BatchHeader *hdr,
                      const long long *__restrict__ box_off, unsigned long long *checks) {
+  extern __shared__ unsigned long long block_checks[];  // SMEM: one per scene
   const long long n = min((long long)hdr->pairs, capacity);
   const int S = hdr->n_scenes;
   const int lane = threadIdx.x & 31;
   const long long warp = (blockIdx.x * 256ll + threadIdx.x) >> 5;
   const long long nwarps = (gridDim.x * 256ll) >> 5;
+  unsigned long long *acc_to = SMEM ? block_checks : checks;
+  if (SMEM) {
+    for (int s = threadIdx.x; s < S; s += 256) block_checks[s] = 0ull;
+    __syncthreads();
+  }
   auto flush = [&](int cur, unsigned long long acc) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) acc ^= __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0 && cur >= 0 && acc) atomicXor(&checks[cur], acc);
+    if (lane == 0 && cur >= 0 && acc) atomicXor(&acc_to[cur], acc);
   };
   for (long long base = warp * kChecksumChunk; base < n; base += nwarps * kChecksumChunk) {
     const long long end = min(base + kChecksumChunk, n);
@@ -130,11 +141,16 @@ pair_checksum_kernel(const int2 *__restrict__ pairs, long long capacity, const B
                                    c = (unsigned long long)(p.y - box_off[t]);
           const unsigned long long h = mix64((a << 32) | c);
           if (in_new) acc ^= h;
-          else atomicXor(&checks[t], h);
+          else atomicXor(&acc_to[t], h);
         }
       }
     }
     flush(cur, acc);
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int s = threadIdx.x; s < S; s += 256)
+      if (block_checks[s]) atomicXor(&checks[s], block_checks[s]);
   }
 }
 
@@ -155,8 +171,12 @@ cudaError_t launch_pair_checksums(cudaStream_t s, const stq_pair *pairs, long lo
   if (e != cudaSuccess) return e;
   int64_t g = (capacity / kChecksumChunk + 7) / 8;  // 8 warps per block
   g = g < 1 ? 1 : (g > 152 * 16 ? 152 * 16 : g);
-  pair_checksum_kernel<<<unsigned(g), 256, 0, s>>>(reinterpret_cast<const int2 *>(pairs), capacity,
-                                                   hdr, box_off, checks);
+  if (scene_cap <= kChecksumSmemScenes)
+    pair_checksum_kernel<true><<<unsigned(g), 256, sizeof(unsigned long long) * size_t(scene_cap), s>>>(
+        reinterpret_cast<const int2 *>(pairs), capacity, hdr, box_off, checks);
+  else
+    pair_checksum_kernel<false><<<unsigned(g), 256, 0, s>>>(reinterpret_cast<const int2 *>(pairs), capacity,
+                                                            hdr, box_off, checks);
   return cudaGetLastError();
 }
 
