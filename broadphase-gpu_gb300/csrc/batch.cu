@@ -18,7 +18,6 @@ namespace stq {
 namespace {
 
 constexpr int kBlock = 256;
-constexpr int kItems = kTileBoxes / kBlock;
 constexpr int kHistBias = 40;  // extent bucket = binary exponent + 40
 constexpr int kSampleBoxes = 1024;
 

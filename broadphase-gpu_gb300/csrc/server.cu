@@ -516,7 +516,6 @@ int stq_server_tick(stq_server *sv, int64_t *done_ids, int max_done, int *n_done
   // 1. admit in arrival order while the head of the queue fits; its upload
   //    overlaps the tick in flight
   int64_t boxes = active_boxes(sv);
-  bool uploaded = false;
   while (!sv->queue.empty()) {
     Request *r = sv->queue.front();
     if (int(sv->active.size()) >= sv->max_scenes || boxes + r->boxes() > sv->max_boxes ||
@@ -529,14 +528,12 @@ int stq_server_tick(stq_server *sv, int64_t *done_ids, int max_done, int *n_done
     }
     STQ_CUDA(sv->ctx, cudaMemcpyAsync(r->dmem, r->host, r->bytes, cudaMemcpyHostToDevice, sv->copy_stream),
              "upload request");
-    uploaded = true;
     sv->held += r->footprint;
     boxes += r->boxes();
     sv->active.push_back(r);
     sv->queue.pop_front();
   }
   STQ_CUDA(sv->ctx, cudaEventRecord(sv->copy_done, sv->copy_stream), "record uploads");
-  (void)uploaded;
   // 2. results of the tick in flight; finished requests leave
   if (sv->in_flight) STQ_TRY(collect(sv, done_ids, max_done, n_done));
   // 3. next tick over the current timestep of every active request
