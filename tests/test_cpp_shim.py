@@ -23,6 +23,17 @@ def test_shim_header_compiles():
                         f"-I{cuda_include()}", str(SRC)], check=True)
 
 
+def test_resume_cursor_covers_every_position_once(tmp_path):
+    """The drop-in's tidstart / MAX_OVERLAP_CUTOFF count start boxes and map
+    onto the prepared positions: any cutoff sequence, halved or not, covers
+    all positions in order, once (host logic: no GPU)."""
+    exe = tmp_path / "cursor_check"
+    subprocess.run(["g++", "-std=c++17", "-Wall", "-Werror", "-O1", f"-I{ROOT / 'include'}", f"-I{cuda_include()}",
+                    str(ROOT / "tests" / "cpp" / "cursor_check.cpp"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", r.stdout + r.stderr
+
+
 def write_mesh(path, mesh):
     with open(path, "wb") as f:
         np.array([mesh.V0.shape[0], mesh.E.shape[0], mesh.F.shape[0]], np.int64).tofile(f)
