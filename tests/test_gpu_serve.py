@@ -63,6 +63,39 @@ def test_large_request_each_timestep_is_exact(stq, oracle, cuda):
     assert first == 0 and last - first + 1 == 3
 
 
+def test_dense_request_outgrows_the_pair_estimate(stq, oracle, cuda):
+    """Two sheets 0.002 apart with large motion find over 40 pairs per box, more
+    than the server's first pair-buffer estimate: the tick grows the buffer and
+    sweeps the step again. Every step still equals the oracle."""
+    mesh = stq.cloth_pair(g=60, z_offset=0.002, sigma=0.03, seed=9)
+    with stq.Server(0, None, budget_bytes=8 << 30, max_boxes=1 << 20, max_scenes=8) as sv:
+        rid = sv.submit(mesh, steps=2, sigma=0.003, seed=12)
+        want = []
+        for step in range(2):
+            sv.tick()
+            V0, V1 = sv.mesh(rid)
+            want.append(oracle_step(stq, oracle, mesh, V0, V1))
+        run_until_done(sv, [rid])
+        counts, checks = sv.result(rid)
+    assert want[0][0] > 25 * mesh.num_boxes
+    assert [int(c) for c in counts] == [w[0] for w in want]
+    assert [int(c) for c in checks] == [w[1] for w in want]
+
+
+def test_many_scene_slots_checksums(stq, oracle, cuda):
+    """A server with more scene slots than the checksum kernel's shared-memory
+    table holds (4,096) adds its checksums straight to global memory; they equal
+    the oracle's."""
+    meshes = [stq.cloth_pair(g=g, z_offset=0.004, sigma=0.004, seed=70 + g) for g in (14, 22, 31)]
+    with stq.Server(0, None, budget_bytes=8 << 30, max_boxes=1 << 18, max_scenes=5000) as sv:
+        ids = [sv.submit(m, steps=1, sigma=0.0, seed=k) for k, m in enumerate(meshes)]
+        run_until_done(sv, ids)
+        for rid, m in zip(ids, meshes):
+            counts, checks = sv.result(rid)
+            want = oracle_step(stq, oracle, m, m.V0, m.V1)
+            assert (int(counts[0]), int(checks[0])) == want
+
+
 @pytest.mark.parametrize("shape", [(1, 8, 1), (4, 0, 1), (8, 0, 1), (1, 4, 2), (1, 2, 2)])
 def test_server_sweep_shapes_agree(stq, cuda, shape):
     """stq_server_set_option retunes the server's sweep (the next tick captures
