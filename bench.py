@@ -196,7 +196,7 @@ def workload_config(name: str, nV: int, nE: int, nF: int) -> dict:
             "l2": "inputs and sorted scene exceed the 129 MB L2; GPU steps also flush L2 (512 MB write)"}
 
 
-def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
+def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush, tune=True, options="", loop=True):
     """256 cloth-pair scenes (box counts log-uniform in [1e3, 2e5]): the fused,
     graph-captured batch call against the per-scene plain launch loop
     (build + prepare + sweep with its host synchronisations, scene by scene),
@@ -212,10 +212,12 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
     total = r.total
     cap = int(total * 1.05) + 1024
     pairs = torch.empty((cap, 2), dtype=torch.int32, device=dev)
-    bboxes = torch.empty((N, 11), dtype=torch.int32, device=dev)
-    bo = ctx.batch_build_boxes(d[0], d[1], vo, d[2], eo, d[3], fo, bboxes)
-    tune_ms, tuned = ctx.autotune(bboxes, bo, pairs, cap)
-    del bboxes
+    tuned, tune_ms = context_options(stq, ctx, options) or "library defaults", None
+    if tune:
+        bboxes = torch.empty((N, 11), dtype=torch.int32, device=dev)
+        bo = ctx.batch_build_boxes(d[0], d[1], vo, d[2], eo, d[3], fo, bboxes)
+        tune_ms, tuned = ctx.autotune(bboxes, bo, pairs, cap)
+        del bboxes
 
     def timed(fn):
         for _ in range(warmup):
@@ -246,7 +248,7 @@ def bench_batched(stq, torch, dev, stream, local, steps, warmup, flush):
             found += ctx.sweep_prepared(pairs, cap).count
         assert found == total, (found, total)
 
-    t_plain = timed(plain_loop)
+    t_plain = timed(plain_loop) if loop else float("nan")
     ctx.close()
     return {"workload": "256 cloth-pair scenes, boxes log-uniform in [1e3, 2e5]", "boxes": N,
             "pairs": int(total), "batched_ms": t_batch, "plain_loop_ms": t_plain,
@@ -494,6 +496,8 @@ def main():
                     help="context options for the main scene, e.g. cell_scale=4,shape=2 (with --no-tune)")
     ap.add_argument("--only-skewed", action="store_true",
                     help="run the skewed 64-scene batch alone and print its figures (profiling runs)")
+    ap.add_argument("--only-batched", action="store_true",
+                    help="run the 256-scene batched call alone, without the per-scene loop (profiling runs)")
     ap.add_argument("--serve-requests", type=int, default=48)
     ap.add_argument("--serve-rates", type=str, default="50,200,500,1000,2000")
     args = ap.parse_args()
@@ -538,6 +542,12 @@ def main():
         if rank == 0:
             print(json.dumps(bench_skewed(stq, torch, dev, stream, local, args.steps, args.warmup, flush,
                                           tune=not args.no_tune, options=args.options)), flush=True)
+        return
+    if args.only_batched:
+        if rank == 0:
+            print(json.dumps(bench_batched(stq, torch, dev, stream, local, args.steps, args.warmup, flush,
+                                           tune=not args.no_tune, options=args.options, loop=False)),
+                  flush=True)
         return
 
     ctx = stq.Context(local, stream.cuda_stream)

@@ -307,8 +307,9 @@ int enqueue_prepare_back(stq_context *ctx, const BatchBuffers &b, int seg_bits, 
   stage_begin(ctx, kSort);
   const int rbits = ctx->options[STQ_OPT_RADIX_BITS] == 4 ? 4 : 8;
   const int64_t r = replicas >= 0 ? replicas : ctx->rep_cap;
+  // seg_bits covers the capacity; passes above the actual list count copy through
   STQ_CUDA(ctx, radix_sort_u64_vals(ctx->stream, kb, vb, r, 32, 32 + std::max(seg_bits, 1), ctx->sort_ws.ptr,
-                                    &which, &ctx->launches, &b.hdr->replicas, rbits),
+                                    &which, &ctx->launches, &b.hdr->replicas, rbits, &b.hdr->lists),
            "launch list sort");
   stage_end(ctx, kSort);
   ctx->scene.xmin = ctx->xmin.as<float>();

@@ -77,6 +77,7 @@ batch_reset_kernel(SceneRecord *scenes, const SceneInput *__restrict__ inputs,
     hdr->flags = 0;
     hdr->replicas = 0;
     hdr->cells = 0;
+    hdr->lists = 0;
     hdr->length = 0;
     hdr->work = 0;
     hdr->pairs = 0;
@@ -400,6 +401,7 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
   if (threadIdx.x == 0) {
     cell_base[S] = carry;
     hdr->cells = carry;
+    hdr->lists = 3u * carry;
   }
 }
 

@@ -27,10 +27,20 @@ static_assert(TileShape<uint32_t>::tile == kRadixTile && TileShape<unsigned long
 
 int64_t num_tiles(int64_t n, int tile) { return (n + tile - 1) / tile; }
 
+// A pass whose digit is 0 in every key: d_hi counts the distinct values of
+// the keys' bits from begin_bit up, rel = shift - begin_bit.
+__device__ __forceinline__ bool pass_is_identity(const unsigned int *d_hi, int rel) {
+  if (!d_hi) return false;
+  const unsigned int hi = *d_hi;
+  return rel >= 32 || hi <= 1u || ((hi - 1u) >> rel) == 0u;
+}
+
 template <typename K, int BITS>
 __global__ void __launch_bounds__(kSortBlock)
 upsweep_kernel(const K *__restrict__ keys, int64_t n, int shift,
-               uint32_t *__restrict__ hist, int64_t ntiles, const unsigned int *d_n, bool match) {
+               uint32_t *__restrict__ hist, int64_t ntiles, const unsigned int *d_n, bool match,
+               const unsigned int *d_hi, int rel) {
+  if (pass_is_identity(d_hi, rel)) return;  // the scatter copies the keys through
   if (d_n && int64_t(*d_n) < n) n = *d_n;
   constexpr int BINS = 1 << BITS;
   constexpr int TILE = TileShape<K>::tile;
@@ -163,11 +173,20 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
                  const uint32_t *__restrict__ vin, uint32_t *__restrict__ vout,
                  int64_t n, int shift, const uint32_t *__restrict__ tile_off,
                  const uint32_t *__restrict__ digit_base, int64_t ntiles,
-                 const unsigned int *d_n) {
+                 const unsigned int *d_n, const unsigned int *d_hi, int rel) {
   if (d_n && int64_t(*d_n) < n) n = *d_n;
   constexpr int BINS = 1 << BITS;
   constexpr int ITEMS = TileShape<K>::items;
   constexpr int TILE = TileShape<K>::tile;
+  if (pass_is_identity(d_hi, rel)) {
+    // every key's digit is 0: the stable pass is the identity; copy the tile
+    const int64_t t0 = int64_t(blockIdx.x) * TILE;
+    for (int64_t i = t0 + threadIdx.x; i < n && i < t0 + TILE; i += kSortBlock) {
+      kout[i] = kin[i];
+      if (VALS) vout[i] = vin[i];
+    }
+    return;
+  }
   __shared__ uint32_t cnt[kSortWarps][BINS + 1];
   __shared__ uint32_t tile_prefix[BINS];
   __shared__ uint32_t gbase[BINS];
@@ -260,7 +279,8 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
 template <typename K, int BITS, bool VALS>
 cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
                       int begin_bit, int end_bit, void *workspace, int *which,
-                      int64_t *launches, const unsigned int *d_n = nullptr) {
+                      int64_t *launches, const unsigned int *d_n = nullptr,
+                      const unsigned int *d_hi = nullptr) {
   constexpr int BINS = 1 << BITS;
   constexpr int TILE = TileShape<K>::tile;
   *which = 0;
@@ -273,12 +293,13 @@ cudaError_t sort_impl(cudaStream_t s, K *kbuf[2], uint32_t *vbuf[2], int64_t n,
     // the top digit of 4-byte keys (float sign and exponent) repeats within warps
     const bool match = sizeof(K) == 4 && shift + BITS >= 32;
     upsweep_kernel<K, BITS><<<unsigned(ntiles), kSortBlock, 0, s>>>(kbuf[cur], n, shift,
-                                                                     hist, ntiles, d_n, match);
+                                                                     hist, ntiles, d_n, match, d_hi,
+                                                                     shift - begin_bit);
     scan_rows_kernel<<<BINS, kSortBlock, 0, s>>>(hist, ntiles, totals);
     scan_totals_kernel<BINS><<<1, kSortBlock, 0, s>>>(totals);
     downsweep_kernel<K, BITS, VALS><<<unsigned(ntiles), kSortBlock, 0, s>>>(
         kbuf[cur], kbuf[cur ^ 1], VALS ? vbuf[cur] : nullptr,
-        VALS ? vbuf[cur ^ 1] : nullptr, n, shift, hist, totals, ntiles, d_n);
+        VALS ? vbuf[cur ^ 1] : nullptr, n, shift, hist, totals, ntiles, d_n, d_hi, shift - begin_bit);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (launches) *launches += 4;
@@ -314,12 +335,12 @@ cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2], int64_t 
 cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2], uint32_t *vbuf[2],
                                 int64_t n, int begin_bit, int end_bit, void *workspace,
                                 int *which, int64_t *launches, const unsigned int *d_n,
-                                int bits) {
+                                int bits, const unsigned int *d_hi) {
   if (bits == 4)
     return sort_impl<unsigned long long, 4, true>(s, kbuf, vbuf, n, begin_bit, end_bit,
-                                                  workspace, which, launches, d_n);
+                                                  workspace, which, launches, d_n, d_hi);
   return sort_impl<unsigned long long, 8, true>(s, kbuf, vbuf, n, begin_bit, end_bit,
-                                                workspace, which, launches, d_n);
+                                                workspace, which, launches, d_n, d_hi);
 }
 
 // ---- exclusive scan of uint32 counts (reduce-then-scan, no waiting) -------------

@@ -121,6 +121,8 @@ struct BatchHeader {
   unsigned int max_list;    // longest (cell, type) list
   unsigned int box_count;   // input: n_boxes as the element count of the box sort
   unsigned long long candidates;  // candidates tested by the last sweep
+  unsigned int lists;       // (cell, type) lists: 3 * cells
+  unsigned int pad;
 };
 
 // A tile of at most kTileBoxes consecutive boxes of one scene (built by the
@@ -308,10 +310,16 @@ cudaError_t radix_sort_u32(cudaStream_t s, uint32_t *kbuf[2], uint32_t *vbuf[2],
 cudaError_t radix_sort_u64(cudaStream_t s, unsigned long long *kbuf[2],
                            int64_t n, int begin_bit, int end_bit, void *workspace,
                            int *which, int64_t *launches);
+// d_hi (may be null): on the device, the number of distinct values of the
+// keys' bits from begin_bit up; a pass whose digit is 0 in every key (all those
+// values below 2^(its shift - begin_bit)) copies the keys through instead of
+// ranking them, so a sort sized for a capacity (a captured graph) pays for
+// the digits the actual keys use.
 cudaError_t radix_sort_u64_vals(cudaStream_t s, unsigned long long *kbuf[2],
                                 uint32_t *vbuf[2], int64_t n, int begin_bit, int end_bit,
                                 void *workspace, int *which, int64_t *launches,
-                                const unsigned int *d_n = nullptr, int bits = 8);
+                                const unsigned int *d_n = nullptr, int bits = 8,
+                                const unsigned int *d_hi = nullptr);
 // exclusive scan of n uint32 counts; *d_total receives the sum
 size_t scan_workspace_bytes(int64_t n);
 cudaError_t exclusive_scan_u32(cudaStream_t s, const uint32_t *in, uint32_t *out, int64_t n,
