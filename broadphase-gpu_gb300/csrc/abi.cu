@@ -286,7 +286,7 @@ int enqueue_prepare_front(stq_context *ctx, const BatchBuffers &b, int64_t n_box
   STQ_CUDA(ctx, exclusive_scan_u32(ctx->stream, b.counts, b.offsets, ctx->box_cap, ctx->scan_ws.ptr,
                                    &b.hdr->replicas, &ctx->launches),
            "launch replica scan");
-  ctx->launches += 7;  // reset, statistics, policy, levels, choose, box keys, counts
+  ctx->launches += 6;  // reset, statistics, policy, box keys, choose, counts
   return STQ_OK;
 }
 
@@ -702,7 +702,7 @@ int stq_select_axis(stq_context *ctx, const stq_aabb *d_boxes, int64_t n, int *a
   BatchBuffers b = batch_buffers(ctx, d_boxes);
   STQ_CUDA(ctx, launch_batch_stats(ctx->stream, b), "launch statistics");
   STQ_CUDA(ctx, launch_batch_policy(ctx->stream, b), "launch policy");
-  ctx->launches += 5;
+  ctx->launches += 3;
   STQ_TRY(read_header(ctx));
   *axis_out = ctx->h_hdr->axis;
   return STQ_OK;

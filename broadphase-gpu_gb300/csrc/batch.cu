@@ -10,6 +10,10 @@
 //
 // All sizes are read from the BatchHeader on the device, so one captured
 // graph serves any batch within the buffer capacities.
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "stq_device.cuh"
 #include "stq_internal.h"
 
@@ -90,11 +94,7 @@ __global__ void __launch_bounds__(kBlock)
 batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
                    SceneRecord *scenes, BatchHeader *hdr) {
   if (int(blockIdx.x) >= hdr->n_tiles) return;
-  constexpr int W = 11;  // words per box
-  __shared__ uint32_t stage[kBlock / 32][32 * W];
   const TileRec t = tiles[blockIdx.x];
-  const int lane = threadIdx.x & 31;
-  uint32_t *sm = stage[threadIdx.x >> 5];
   // moments about the tile's first box centre, in fp32 per thread (fp64 is
   // slow on this part); the block combines them in fp64 and shifts them back
   float c[3];
@@ -106,59 +106,78 @@ batch_stats_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict
   float s1[3] = {0.f, 0.f, 0.f}, s2[3] = {0.f, 0.f, 0.f};
   uint32_t lo[3] = {0xffffffffu, 0xffffffffu, 0xffffffffu}, hi[3] = {0u, 0u, 0u};
   bool inverted = false, nan = false;
-  // warp-staged loads: 32 boxes as 11 coalesced word loads, all issued before
-  // the first is stored (a store that waits on its load would serialise them)
-  const uint32_t *src = reinterpret_cast<const uint32_t *>(boxes + t.begin);
-  for (int i0 = threadIdx.x - lane; i0 < t.count; i0 += kBlock) {
-    const int n = min(32, t.count - i0);
-    if (n == 32) {
-      uint32_t v[W];
+  // thread i takes boxes i, i + kBlock, ...: each warp load instruction covers
+  // 32 consecutive boxes, and the unrolled loop keeps several boxes in flight
+  const stq_aabb *tb = boxes + t.begin;
+#pragma unroll 4
+  for (int i = threadIdx.x; i < t.count; i += kBlock) {
+    const stq_aabb &x = tb[i];
+    float l[3], h[3];
 #pragma unroll
-      for (int w = 0; w < W; ++w) v[w] = src[int64_t(i0) * W + w * 32 + lane];
+    for (int k = 0; k < 3; ++k) l[k] = x.min[k], h[k] = x.max[k];
 #pragma unroll
-      for (int w = 0; w < W; ++w) sm[w * 32 + lane] = v[w];
-    } else {
-      for (int w = lane; w < n * W; w += 32) sm[w] = src[int64_t(i0) * W + w];
+    for (int k = 0; k < 3; ++k) {
+      nan |= (l[k] != l[k]) | (h[k] != h[k]);
+      inverted |= l[k] > h[k];
+      const float dl = l[k] - c[k], dh = h[k] - c[k];
+      s1[k] += dl + dh;
+      s2[k] += dl * dl + dh * dh;
+      lo[k] = min(lo[k], float_key(l[k]));
+      hi[k] = max(hi[k], float_key(h[k]));
     }
-    __syncwarp();
-    if (lane < n) {
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        const float l = __uint_as_float(sm[lane * W + 1 + k]), h = __uint_as_float(sm[lane * W + 4 + k]);
-        nan |= (l != l) | (h != h);
-        inverted |= l > h;
-        const float dl = l - c[k], dh = h - c[k];
-        s1[k] += dl + dh;
-        s2[k] += dl * dl + dh * dh;
-        lo[k] = min(lo[k], float_key(l));
-        hi[k] = max(hi[k], float_key(h));
-      }
-    }
-    __syncwarp();
   }
-  __shared__ double dred[kBlock / 32][6];
-  SceneRecord &r = scenes[t.scene];
-  const double mom[6] = {double(s1[0]), double(s1[1]), double(s1[2]), double(s2[0]), double(s2[1]), double(s2[2])};
-  double tot[6];
-  block_sums(mom, tot, dred);
+  // warp sums in fp32 (a fixed shuffle tree); the 8 warp sums of each moment
+  // are combined in fp64 by one lane each, and each value reaches the scene
+  // record with one atomic per block (fp64 and same-address atomics are slow)
+  constexpr int kWarps = kBlock / 32;
+  __shared__ float wsum[6][kWarps];
+  __shared__ uint32_t wkey[6][kWarps];
+  __shared__ int wflag[kWarps];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float m[6] = {s1[0], s1[1], s1[2], s2[0], s2[1], s2[2]};
+#pragma unroll
+  for (int k = 0; k < 6; ++k)
+    for (int o = 16; o > 0; o >>= 1) m[k] += __shfl_down_sync(kFullMask, m[k], o);
+  uint32_t kk[6];
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    // sum(l + h) = S1 + 2 n c; sum(l^2 + h^2) = S2 + 2 c S1 + 2 n c^2
-    if (threadIdx.x == 0) {
-      const double a = tot[k], q = tot[3 + k];
-      const double ck = c[k], n = double(t.count);
-      atomicAdd(&r.s1[k], a + 2.0 * n * ck);
-      atomicAdd(&r.s2[k], q + 2.0 * ck * a + 2.0 * n * ck * ck);
-    }
-    const uint32_t l = __reduce_min_sync(kFullMask, lo[k]);
-    const uint32_t h = __reduce_max_sync(kFullMask, hi[k]);
-    if ((threadIdx.x & 31) == 0) {
-      atomicMin(&r.lo_key[k], l);
-      atomicMax(&r.hi_key[k], h);
+    kk[k] = __reduce_min_sync(kFullMask, lo[k]);
+    kk[3 + k] = __reduce_max_sync(kFullMask, hi[k]);
+  }
+  const int fl = (__any_sync(kFullMask, inverted) ? 1 : 0) | (__any_sync(kFullMask, nan) ? 2 : 0);
+  if (lane == 0) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) wsum[k][warp] = m[k], wkey[k][warp] = kk[k];
+    wflag[warp] = fl;
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  SceneRecord &r = scenes[t.scene];
+  double tot = 0.0;  // lane k < 6: moment k of the block
+  uint32_t key = lane < 3 ? 0xffffffffu : 0u;  // lanes 0-2 minima, 3-5 maxima
+  int flags = 0;
+  if (lane < 6) {
+    for (int w = 0; w < kWarps; ++w) {
+      tot += double(wsum[lane][w]);
+      key = lane < 3 ? min(key, wkey[lane][w]) : max(key, wkey[lane][w]);
+      flags |= wflag[w];
     }
   }
-  if (__any_sync(kFullMask, inverted) && (threadIdx.x & 31) == 0) atomicOr(&r.inverted, 1);
-  if (__any_sync(kFullMask, nan) && (threadIdx.x & 31) == 0) atomicOr(&hdr->flags, kFlagNaN);
+  // sum(l + h) = S1 + 2 n c; sum(l^2 + h^2) = S2 + 2 c S1 + 2 n c^2
+  const double a1 = __shfl_sync(kFullMask, tot, lane < 3 ? lane : lane - 3);
+  if (lane < 6) {
+    const int k = lane < 3 ? lane : lane - 3;
+    const double ck = k == 0 ? c[0] : (k == 1 ? c[1] : c[2]), n = double(t.count);
+    if (lane < 3) {
+      atomicAdd(&r.s1[k], tot + 2.0 * n * ck);
+      atomicMin(&r.lo_key[k], key);
+    } else {
+      atomicAdd(&r.s2[k], tot + 2.0 * ck * a1 + 2.0 * n * ck * ck);
+      atomicMax(&r.hi_key[k], key);
+    }
+  }
+  if (lane == 0 && (flags & 1)) atomicOr(&r.inverted, 1);
+  if (lane == 0 && (flags & 2)) atomicOr(&hdr->flags, kFlagNaN);
 }
 
 __device__ int grid_side(float L, float h) {
@@ -167,10 +186,7 @@ __device__ int grid_side(float L, float h) {
   return s > float(kMaxGridSide) ? kMaxGridSide : (s < 1.f ? 1 : int(s));
 }
 
-__device__ __forceinline__ int level_side(int base, int level) {
-  const int s = (base + (1 << level) - 1) >> level;
-  return s < 1 ? 1 : s;
-}
+__device__ __forceinline__ float inv_side(int n, float L) { return n > 1 ? float(n) / L : 0.f; }
 
 // ---- 2. policy: one block per scene ---------------------------------------------
 // Sweep axis of largest corner variance (x, then y, preferred on ties, as
@@ -257,14 +273,16 @@ batch_policy_kernel(const stq_aabb *__restrict__ boxes, const long long *__restr
   }
   if (!(Lb > 0.f) || !isfinite(Lb)) nb = 1;
   if (!(Lc > 0.f) || !isfinite(Lc)) nc = 1;
-  r.base_nb = nb;
-  r.base_nc = nc;
   GridParams &g = r.grid;
   g.axis = axis;
   g.ob = lob;
   g.oc = loc;
   g.Lb = Lb;
   g.Lc = Lc;
+  g.ib = inv_side(nb, Lb);
+  g.ic = inv_side(nc, Lc);
+  g.nb0 = g.ib == 0.f ? 1 : nb;
+  g.nc0 = g.ic == 0.f ? 1 : nc;
   if (s == 0) hdr->axis = axis;
 }
 
@@ -284,7 +302,6 @@ __device__ __forceinline__ Range cell_range(const stq_aabb &x, int a, float ob, 
   return r;
 }
 
-__device__ __forceinline__ float inv_side(int n, float L) { return n > 1 ? float(n) / L : 0.f; }
 
 // Scene of box bi: the last scene whose first box is <= bi.
 __device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, int S, uint32_t bi) {
@@ -295,46 +312,6 @@ __device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, i
     else hi = mid - 1;
   }
   return lo;
-}
-
-// ---- 3. replicas per grid level, per scene ------------------------------------------
-__global__ void __launch_bounds__(kBlock)
-batch_levels_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
-                    SceneRecord *scenes, const BatchHeader *hdr) {
-  if (int(blockIdx.x) >= hdr->n_tiles) return;
-  const TileRec t = tiles[blockIdx.x];
-  SceneRecord &r = scenes[t.scene];
-  const GridParams g = r.grid;
-  int nbl[kGridLevels], ncl[kGridLevels];
-  float ibl[kGridLevels], icl[kGridLevels];
-#pragma unroll
-  for (int l = 0; l < kGridLevels; ++l) {
-    nbl[l] = level_side(r.base_nb, l);
-    ncl[l] = level_side(r.base_nc, l);
-    ibl[l] = inv_side(nbl[l], g.Lb);
-    icl[l] = inv_side(ncl[l], g.Lc);
-  }
-  // a thread sees at most kTileBoxes / kBlock = 16 boxes of at most 2048^2
-  // cells each: 32-bit sums per thread, 64-bit per block
-  static_assert(uint64_t(kTileBoxes / kBlock) * kMaxGridSide * kMaxGridSide < (uint64_t(1) << 32),
-                "per-thread level sums");
-  unsigned reps[kGridLevels] = {};
-  for (int i = threadIdx.x; i < t.count; i += kBlock) {
-    const stq_aabb &x = boxes[t.begin + i];
-#pragma unroll
-    for (int l = 0; l < kGridLevels; ++l) {
-      const Range q = cell_range(x, g.axis, g.ob, ibl[l], nbl[l], g.oc, icl[l], ncl[l]);
-      reps[l] += unsigned(q.b1 - q.b0 + 1) * unsigned(q.c1 - q.c0 + 1);
-    }
-  }
-  __shared__ unsigned long long red[kBlock / 32][kGridLevels];
-  unsigned long long wide[kGridLevels], tot[kGridLevels];
-#pragma unroll
-  for (int l = 0; l < kGridLevels; ++l) wide[l] = reps[l];
-  block_sums(wide, tot, red);
-  if (threadIdx.x == 0)
-#pragma unroll
-    for (int l = 0; l < kGridLevels; ++l) atomicAdd(&r.level_reps[l], tot[l]);
 }
 
 // ---- 4. choose the finest level within the replica budget; cell bases ----------
@@ -354,7 +331,7 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
     if (s < S) {
       SceneRecord &r = scenes[s];
       const long long n = box_off[s + 1] - box_off[s];
-      int level = kGridLevels;  // none fits: one cell
+      int level = kCoordBits;  // none fits: every coordinate shifts to cell 0
       if (r.cells_opt > 1) {
         level = 0;  // a requested grid is kept as is
       } else {
@@ -365,13 +342,9 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
           }
       }
       GridParams &g = r.grid;
-      g.level = level;
-      g.nb = level < kGridLevels ? level_side(r.base_nb, level) : 1;
-      g.nc = level < kGridLevels ? level_side(r.base_nc, level) : 1;
-      g.ib = inv_side(g.nb, g.Lb);
-      g.ic = inv_side(g.nc, g.Lc);
-      if (g.ib == 0.f) g.nb = 1;
-      if (g.ic == 0.f) g.nc = 1;
+      g.shift = level;
+      g.nb = ((g.nb0 - 1) >> level) + 1;
+      g.nc = ((g.nc0 - 1) >> level) + 1;
       g.ncells = g.nb * g.nc;
       cells = unsigned(g.ncells);
     }
@@ -406,18 +379,23 @@ batch_choose_kernel(const long long *__restrict__ box_off, SceneRecord *scenes,
 }
 
 // ---- 5. per-box replica counts in sweep-axis order (zero past the last box, up
-// to the capacity), from the cell ranges by box index that the box-key kernel
-// wrote
-__device__ __forceinline__ uint32_t cells_count(uint2 r) {
-  return ((r.x >> 11 & 2047u) - (r.x & 2047u) + 1u) * ((r.y >> 11 & 2047u) - (r.y & 2047u) + 1u);
+// to the capacity), from the level-0 cell ranges by box index that the
+// box-key kernel wrote, at the scene's chosen level
+__device__ __forceinline__ uint32_t cells_count(uint2 r, int shift) {
+  return (((r.x >> 11 & 2047u) >> shift) - ((r.x & 2047u) >> shift) + 1u) *
+         (((r.y >> 11 & 2047u) >> shift) - ((r.y & 2047u) >> shift) + 1u);
 }
 
 __global__ void __launch_bounds__(kBlock)
 batch_count_kernel(const uint32_t *__restrict__ order, const uint2 *__restrict__ box_cells,
+                   const long long *__restrict__ box_off, const SceneRecord *__restrict__ scenes,
                    const BatchHeader *hdr, uint32_t *__restrict__ counts, long long box_cap) {
   const long long N = hdr->n_boxes;
-  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock)
-    counts[p] = cells_count(box_cells[order[p]]);
+  const int S = hdr->n_scenes;
+  for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
+    const uint32_t bi = order[p];
+    counts[p] = cells_count(box_cells[bi], scenes[scene_of(box_off, S, bi)].grid.shift);
+  }
   // positions past the batch contribute nothing to the scan
   for (long long i = N + blockIdx.x * (long long)kBlock + threadIdx.x; i < box_cap;
        i += (long long)gridDim.x * kBlock)
@@ -453,13 +431,13 @@ batch_emit_kernel(const uint2 *__restrict__ box_cells, const uint32_t *__restric
   for (long long p = blockIdx.x * (long long)kBlock + threadIdx.x; p < N; p += (long long)gridDim.x * kBlock) {
     const uint32_t bi = order[p];
     const int sc = scene_of(box_off, S, bi);
-    const int nc = scenes[sc].grid.nc;
+    const int nc = scenes[sc].grid.nc, sh = scenes[sc].grid.shift;
     const unsigned long long cb0 = cell_base[sc];
-    // the box's cell range and type (8 bytes, by box index) and its sort key,
-    // instead of the 44-byte box
+    // the box's level-0 cell range and type (8 bytes, by box index) and its
+    // sort key, instead of the 44-byte box
     const uint2 r = box_cells[bi];
-    const int b0 = int(r.x & 2047u), b1 = int(r.x >> 11 & 2047u);
-    const int c0 = int(r.y & 2047u), c1 = int(r.y >> 11 & 2047u);
+    const int b0 = int(r.x & 2047u) >> sh, b1 = int(r.x >> 11 & 2047u) >> sh;
+    const int c0 = int(r.y & 2047u) >> sh, c1 = int(r.y >> 11 & 2047u) >> sh;
     const unsigned long long type = r.x >> 22;
     const unsigned long long xk = sorted_keys[p];
     uint32_t o = offsets[p];
@@ -473,28 +451,45 @@ batch_emit_kernel(const uint2 *__restrict__ box_cells, const uint32_t *__restric
   }
 }
 
-// Sort keys of the boxes: the order-preserving image of the minimum on the
-// scene's sweep axis, with the box index as value.
+// ---- 3. sort keys of the boxes (the order-preserving image of the minimum on
+// the scene's sweep axis, with the box index as value), each box's level-0
+// cell range and type, and the replicas of every grid level, per scene
 __global__ void __launch_bounds__(kBlock)
 batch_box_keys_kernel(const stq_aabb *__restrict__ boxes, const TileRec *__restrict__ tiles,
-                      const SceneRecord *__restrict__ scenes, const BatchHeader *hdr,
+                      SceneRecord *scenes, const BatchHeader *hdr,
                       uint32_t *__restrict__ keys, uint32_t *__restrict__ vals, uint2 *__restrict__ box_cells) {
   if (int(blockIdx.x) >= hdr->n_tiles) return;
   const TileRec t = tiles[blockIdx.x];
-  const GridParams g = scenes[t.scene].grid;
+  SceneRecord &r = scenes[t.scene];
+  const GridParams g = r.grid;
+  // a thread sees at most kTileBoxes / kBlock = 16 boxes of at most 2048^2
+  // cells each: 32-bit sums per thread, 64-bit per block
+  static_assert(uint64_t(kTileBoxes / kBlock) * kMaxGridSide * kMaxGridSide < (uint64_t(1) << 32),
+                "per-thread level sums");
+  unsigned reps[kGridLevels] = {};
   for (int i = threadIdx.x; i < t.count; i += kBlock) {
     const long long bi = t.begin + i;
     const stq_aabb &x = boxes[bi];
     keys[bi] = float_key(x.min[g.axis]);
     vals[bi] = uint32_t(bi);
     // the box's cell range and type, by box index, while the box is read in
-    // order (cell coordinates are below kMaxGridSide: 11 bits)
-    static_assert(kMaxGridSide <= 2048, "11-bit cell coordinates");
-    const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb, g.oc, g.ic, g.nc);
+    // order (level-0 coordinates fit kCoordBits = 11 bits)
+    const Range q = cell_range(x, g.axis, g.ob, g.ib, g.nb0, g.oc, g.ic, g.nc0);
     const unsigned type = unsigned(type_of(x.vertex_ids[1], x.vertex_ids[2]));
     box_cells[bi] = make_uint2(unsigned(q.b0) | unsigned(q.b1) << 11 | type << 22,
                                unsigned(q.c0) | unsigned(q.c1) << 11);
+#pragma unroll
+    for (int l = 0; l < kGridLevels; ++l)
+      reps[l] += unsigned((q.b1 >> l) - (q.b0 >> l) + 1) * unsigned((q.c1 >> l) - (q.c0 >> l) + 1);
   }
+  __shared__ unsigned long long red[kBlock / 32][kGridLevels];
+  unsigned long long wide[kGridLevels], tot[kGridLevels];
+#pragma unroll
+  for (int l = 0; l < kGridLevels; ++l) wide[l] = reps[l];
+  block_sums(wide, tot, red);
+  if (threadIdx.x == 0)
+#pragma unroll
+    for (int l = 0; l < kGridLevels; ++l) atomicAdd(&r.level_reps[l], tot[l]);
 }
 
 // First position of every (cell, type) list in the sorted replicas, and one
@@ -565,8 +560,9 @@ cell_floor_kernel(const unsigned int *__restrict__ cell_base, const SceneRecord 
     const GridParams g = scenes[lo].grid;
     const int local = int(cell - cell_base[lo]);
     const int cb = local / g.nc, cc = local - cb * g.nc;
-    cell_floor[cell] = make_float2(cb > 0 ? cell_lower_bound(cb, g.ob, g.ib) : -INFINITY,
-                                   cc > 0 ? cell_lower_bound(cc, g.oc, g.ic) : -INFINITY);
+    // cell cb of the chosen level starts at level-0 cell cb << shift
+    cell_floor[cell] = make_float2(cb > 0 ? cell_lower_bound(cb << g.shift, g.ob, g.ib) : -INFINITY,
+                                   cc > 0 ? cell_lower_bound(cc << g.shift, g.oc, g.ic) : -INFINITY);
   }
 }
 
@@ -619,8 +615,8 @@ gather_cells_kernel(const stq_aabb *__restrict__ boxes, const unsigned long long
     const stq_aabb &x = boxes[bi];
     const int local = int(cell - cell_base[lo]);
     const int cb = local / g.nc, cc = local - cb * g.nc;
-    const int fb = cell_coord(x.min[b], g.ob, g.ib, g.nb) == cb;
-    const int fc = cell_coord(x.min[c], g.oc, g.ic, g.nc) == cc;
+    const int fb = (cell_coord(x.min[b], g.ob, g.ib, g.nb0) >> g.shift) == cb;
+    const int fc = (cell_coord(x.min[c], g.oc, g.ic, g.nc0) >> g.shift) == cc;
     const int64_t k = p + seg;
     int64_t first = k + 1;
     // the candidate list: the edge's own list after it, or the other type's
@@ -682,6 +678,36 @@ int blocks_for(int64_t n, int cap = 152 * 16) {
   return int(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
+// Blocks of kBlock threads of a grid-stride kernel over n items: one per
+// kBlock items, at most one wave of resident blocks. Every block of a grid-
+// stride loop takes the same share, so a grid of 2.7 waves would run its last
+// wave on two thirds of the block slots.
+int wave_blocks(const void *kernel, int64_t n) {
+  static std::mutex m;
+  static std::vector<std::pair<const void *, int>> per_sm;  // kernel -> resident blocks per SM
+  int resident = 0;
+  {
+    std::lock_guard<std::mutex> g(m);
+    for (const auto &e : per_sm)
+      if (e.first == kernel) resident = e.second;
+    if (!resident) {
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&resident, kernel, kBlock, 0) != cudaSuccess ||
+          resident < 1) {
+        (void)cudaGetLastError();
+        resident = 1;
+      }
+      per_sm.emplace_back(kernel, resident);
+    }
+  }
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      sms < 1) {
+    (void)cudaGetLastError();
+    sms = 152;
+  }
+  return blocks_for(n, sms * resident);
+}
+
 __global__ void __launch_bounds__(kBlock)
 reset_sweep_kernel(BatchHeader *hdr, unsigned long long *scene_pairs) {
   const int S = hdr->n_scenes;
@@ -731,27 +757,27 @@ cudaError_t launch_batch_stats(cudaStream_t s, const BatchBuffers &b) {
 
 cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b) {
   batch_policy_kernel<<<unsigned(b.scene_cap), kBlock, 0, s>>>(b.boxes, b.box_off, b.scenes, b.hdr);
-  batch_levels_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr);
-  batch_choose_kernel<<<1, 1024, 0, s>>>(b.box_off, b.scenes, b.cell_base, b.hdr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b) {
   batch_box_keys_kernel<<<unsigned(b.tile_cap), kBlock, 0, s>>>(b.boxes, b.tiles, b.scenes, b.hdr, b.box_keys,
                                                                 b.box_vals, b.box_cells);
+  batch_choose_kernel<<<1, 1024, 0, s>>>(b.box_off, b.scenes, b.cell_base, b.hdr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_counts(cudaStream_t s, const BatchBuffers &b, int64_t n) {
-  batch_count_kernel<<<blocks_for(std::max<int64_t>(n, b.box_cap)), kBlock, 0, s>>>(b.order, b.box_cells, b.hdr,
-                                                                                  b.counts, b.box_cap);
+  const int64_t m = std::max<int64_t>(n, b.box_cap);
+  batch_count_kernel<<<wave_blocks((const void *)batch_count_kernel, m), kBlock, 0, s>>>(
+      b.order, b.box_cells, b.box_off, b.scenes, b.hdr, b.counts, b.box_cap);
   return cudaGetLastError();
 }
 
 cudaError_t launch_batch_emit(cudaStream_t s, const BatchBuffers &b, int64_t n, int num_sms) {
-  batch_emit_kernel<<<blocks_for(n), kBlock, 0, s>>>(b.box_cells, b.sorted_keys, b.order, b.box_off, b.scenes,
-                                                     b.cell_base, b.hdr,
-                                              b.offsets, b.keys, b.vals, b.rep_cap, b.seg_cap);
+  batch_emit_kernel<<<wave_blocks((const void *)batch_emit_kernel, n), kBlock, 0, s>>>(
+      b.box_cells, b.sorted_keys, b.order, b.box_off, b.scenes, b.cell_base, b.hdr, b.offsets, b.keys, b.vals,
+      b.rep_cap, b.seg_cap);
   return cudaGetLastError();
 }
 
@@ -768,11 +794,9 @@ cudaError_t launch_gather_cells(cudaStream_t s, const stq_aabb *boxes,
                                 const uint32_t *seg_scan, float2 *cell_floor, int64_t cells_cap,
                                 SortedScene scene) {
   cell_floor_kernel<<<blocks_for(cells_cap), kBlock, 0, s>>>(cell_base, scenes, hdr, cell_floor, cells_cap);
-  gather_cells_kernel<<<blocks_for(rep_cap), kBlock, 0, s>>>(boxes, keys, order, hdr, cell_base,
-                                                             scenes, seg_scan, scene.xmin, scene.xmax,
-                                                             cell_floor, scene.syz, scene.sv,
-                                                             scene.sflag, scene.sfloor, scene.partner,
-                                                             scene.run_end);
+  gather_cells_kernel<<<wave_blocks((const void *)gather_cells_kernel, rep_cap), kBlock, 0, s>>>(
+      boxes, keys, order, hdr, cell_base, scenes, seg_scan, scene.xmin, scene.xmax, cell_floor, scene.syz,
+      scene.sv, scene.sflag, scene.sfloor, scene.partner, scene.run_end);
   return cudaGetLastError();
 }
 

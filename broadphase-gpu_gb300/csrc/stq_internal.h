@@ -60,18 +60,26 @@ constexpr int kMaxGridSide = 2048;
 // cell coordinates are a monotone function of the bound, so a pair that
 // overlaps shares the cell of its reference point (max of mins on b and c)
 // and is emitted there only.
+// The policy sets the level-0 grid (nb0 x nc0 cells of the automatic side, or
+// the requested grid); a cell of level L is a block of 2^L x 2^L level-0
+// cells, and the level is chosen against the replica budget once the box-key
+// pass has counted every level's replicas.
 struct GridParams {
   int axis;       // sweep axis a
-  int nb, nc;     // cells along b and c
+  int nb, nc;     // cells along b and c at the chosen level
   int ncells;     // nb * nc
   float ob, oc;   // grid origin on b and c
-  float ib, ic;   // cells per unit length on b and c
+  float ib, ic;   // level-0 cells per unit length on b and c
   float Lb, Lc;   // extent of the scene on b and c
-  int level;      // grid level chosen against the replica budget
+  int nb0, nc0;   // level-0 cells along b and c
+  int shift;      // cell coordinate = level-0 coordinate >> shift (the chosen
+                  // level; kCoordBits when no level fits: one cell)
   int pad;
 };
 
-constexpr int kGridLevels = 6;  // level L halves the base grid L times
+constexpr int kGridLevels = 6;  // level L halves the level-0 grid L times
+constexpr int kCoordBits = 11;  // level-0 cell coordinates are below 2^11
+static_assert(kMaxGridSide <= (1 << kCoordBits), "level-0 cell coordinates fit kCoordBits");
 
 // One scene of a batch: inputs written by the host, the rest computed on the
 // device by the prepare kernels.
@@ -86,7 +94,6 @@ struct SceneRecord {
   unsigned int lo_key[3], hi_key[3];  // order-preserving min / max bounds
   unsigned int hist[3][64];         // log2 histogram of the extents
   int inverted;                     // some box has min > max on an axis
-  int base_nb, base_nc;             // level-0 grid of the policy
   int pad1;
   unsigned long long level_reps[kGridLevels];  // replicas per grid level
   // results
@@ -251,8 +258,12 @@ struct BatchBuffers {
   long long rep_cap;
   int scene_cap;
 };
+// reset and per-scene statistics (2 launches)
 cudaError_t launch_batch_stats(cudaStream_t s, const BatchBuffers &b);
+// sweep axis and level-0 grid per scene (1 launch)
 cudaError_t launch_batch_policy(cudaStream_t s, const BatchBuffers &b);
+// box sort keys, level-0 cell ranges and every level's replica count; then the
+// level within the replica budget and the cell bases (2 launches)
 cudaError_t launch_batch_box_keys(cudaStream_t s, const BatchBuffers &b);
 // n: positions to cover (the box count, or the box capacity when only the
 // device knows the count)
