@@ -192,6 +192,7 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
   __shared__ uint32_t gbase[BINS];
   __shared__ uint32_t scratch[32];
   __shared__ K stage[TILE];
+  __shared__ uint32_t vstage[VALS ? TILE : 1];
   __shared__ uint8_t stage_d[TILE];
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -246,33 +247,24 @@ downsweep_kernel(const K *__restrict__ kin, K *__restrict__ kout,
         digit_base[threadIdx.x] + tile_off[int64_t(threadIdx.x) * ntiles + blockIdx.x];
   }
   __syncthreads();
-  // Stage keys in tile-sorted order, then write them out digit run by run.
-  int pos[ITEMS];
+  // Stage keys and values in tile-sorted order, then write both out digit run
+  // by run (one destination per staged element).
 #pragma unroll
   for (int it = 0; it < ITEMS; ++it) {
     if (dig[it] < BINS) {
-      pos[it] = int(tile_prefix[dig[it]] + cnt[warp][dig[it]] + rank[it]);
-      stage[pos[it]] = key[it];
-      stage_d[pos[it]] = uint8_t(dig[it]);
+      const int pos = int(tile_prefix[dig[it]] + cnt[warp][dig[it]] + rank[it]);
+      stage[pos] = key[it];
+      if (VALS) vstage[pos] = val[it];
+      stage_d[pos] = uint8_t(dig[it]);
     }
   }
   __syncthreads();
   const int count = int(n - tile_start < TILE ? (n > tile_start ? n - tile_start : 0) : TILE);
   for (int p = threadIdx.x; p < count; p += kSortBlock) {
     const int d = stage_d[p];
-    kout[gbase[d] + (p - tile_prefix[d])] = stage[p];
-  }
-  if (VALS) {
-    __syncthreads();
-    uint32_t *vstage = reinterpret_cast<uint32_t *>(stage);
-#pragma unroll
-    for (int it = 0; it < ITEMS; ++it)
-      if (dig[it] < BINS) vstage[pos[it]] = val[it];
-    __syncthreads();
-    for (int p = threadIdx.x; p < count; p += kSortBlock) {
-      const int d = stage_d[p];
-      vout[gbase[d] + (p - tile_prefix[d])] = vstage[p];
-    }
+    const uint32_t o = gbase[d] + (p - tile_prefix[d]);
+    kout[o] = stage[p];
+    if (VALS) vout[o] = vstage[p];
   }
 }
 
