@@ -302,7 +302,6 @@ __device__ __forceinline__ Range cell_range(const stq_aabb &x, int a, float ob, 
   return r;
 }
 
-
 // Scene of box bi: the last scene whose first box is <= bi.
 __device__ __forceinline__ int scene_of(const long long *__restrict__ box_off, int S, uint32_t bi) {
   int lo = 0, hi = S - 1;
