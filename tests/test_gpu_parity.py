@@ -644,6 +644,32 @@ def test_cells_skewed_slivers(ctx, stq, oracle, cuda):
         assert np.array_equal(got, want), scale
 
 
+@pytest.mark.parametrize("shape", [1, 2])
+def test_cells_coarse_levels(ctx, stq, oracle, cuda, shape):
+    """Grid levels above 0. A cell of level L is a 2^L x 2^L block of level-0
+    cells (the level-0 coordinate shifted right by L), with the first-cell rule
+    at the block's lower bounds; when no level fits the replica budget the
+    scene is one cell. Boxes of side 0.03 in the unit cube span about 5 level-0
+    cells at cell scale 1 (a 44 x 44 grid), 2.7 at level 1 and 1.7 at level 2,
+    so budgets 64, 4, 2 and 1 take levels 0, 1, 2 and one cell; each gives the
+    oracle's pairs."""
+    boxes = stq.random_boxes(150_000, sliver_frac=0.0, seed=31)
+    c = 0.5 * (boxes["min"] + boxes["max"])
+    boxes["min"], boxes["max"] = c - np.float32(0.015), c + np.float32(0.015)
+    want = oracle.broadphase(boxes)
+    ctx.set_option(stq.OPT_SWEEP_SHAPE, shape)
+    ctx.set_option(stq.OPT_CELL_SCALE, 1)
+    lists = {}
+    for budget in (64, 4, 2, 1):
+        ctx.set_option(stq.OPT_REPLICA_BUDGET, budget)
+        got = sweep_pairs(ctx, stq, oracle, boxes_dev(boxes, cuda), len(boxes), cuda, -1)
+        assert np.array_equal(got, want), budget
+        stats = ctx.list_stats()
+        assert stats["replicas"] <= budget * len(boxes), budget
+        lists[budget] = stats["lists"]
+    assert lists[64] > lists[4] > lists[2] > lists[1] == 3, lists
+
+
 def test_cells_inverted_and_infinite_boxes(ctx, stq, oracle, cuda):
     boxes = stq.random_boxes(20_000, seed=12)
     c = 0.5 * (boxes["min"] + boxes["max"])
